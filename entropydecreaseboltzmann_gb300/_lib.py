@@ -1,0 +1,141 @@
+"""ctypes binding of libedb.so (the C ABI declared in include/edb.h).
+
+The library is built in-tree by ``entropydecreaseboltzmann_gb300.build.build()``.
+There is no CPU fallback: importing this module when the library is missing
+raises, and every compute call on a host without a usable GPU raises
+``EdbError`` with status EDB_ECUDA.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libedb.so")
+
+EDB_OK = 0
+STATUS = {0: "EDB_OK", 1: "EDB_EINVAL", 2: "EDB_ENOMEM", 3: "EDB_ECUDA", 4: "EDB_ETIMEDOUT",
+          5: "EDB_ENOTREADY", 6: "EDB_EBUSY", 7: "EDB_ENOTFOUND"}
+INDEX_REFERENCE = 0
+INDEX_ALIASED = 1
+R_REFERENCE = 6.62132
+SCHEME_FE, SCHEME_CFE, SCHEME_RK2, SCHEME_SSP3, SCHEME_RK4, SCHEME_DUFORT = range(6)
+
+
+class EdbError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class QCalcDesc(C.Structure):
+    _fields_ = [("N", C.c_int), ("gamma", C.c_double), ("L", C.c_double), ("filter", C.c_int),
+                ("index_mode", C.c_int)]
+
+
+class QCalcInfo(C.Structure):
+    _fields_ = [("N", C.c_int), ("n", C.c_int), ("P", C.c_int), ("NQ", C.c_longlong),
+                ("terms", C.c_longlong), ("B_bytes", C.c_longlong), ("has_B32", C.c_int)]
+
+
+class SolverDesc(C.Structure):
+    _fields_ = [("N", C.c_int), ("R", C.c_double), ("scheme", C.c_int), ("fix_entropy", C.c_int),
+                ("beta", C.c_double), ("kernel", QCalcDesc)]
+
+
+class BatchDesc(C.Structure):
+    _fields_ = [("S", C.c_int), ("N", C.c_int), ("R", C.c_double), ("scheme", C.c_int),
+                ("dt", C.c_double), ("fix_entropy", C.c_int)]
+
+
+_dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
+_vp = C.c_void_p
+_ip = C.POINTER(C.c_int)
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"{LIB_PATH} is missing: build it with entropydecreaseboltzmann_gb300.build.build() "
+            "(there is no CPU fallback)")
+    L = C.CDLL(LIB_PATH)
+    sig = {
+        "edb_last_error": (C.c_char_p, []),
+        "edb_status_string": (C.c_char_p, [C.c_int]),
+        "edb_version": (C.c_int, []),
+        "edb_kernel_launch_count": (C.c_longlong, []),
+        "edb_measure_fp32_peak": (C.c_int, [_dp]),
+        "edb_qcalc_desc_init": (C.c_int, [C.POINTER(QCalcDesc), C.c_int, C.c_int]),
+        "edb_qcalc_create": (C.c_int, [C.POINTER(QCalcDesc), C.POINTER(_vp)]),
+        "edb_qcalc_destroy": (C.c_int, [_vp]),
+        "edb_qcalc_close_filter": (C.c_int, [_vp]),
+        "edb_qcalc_genB": (C.c_int, [_vp]),
+        "edb_qcalc_calQ": (C.c_int, [_vp, _dp, _dp]),
+        "edb_qcalc_calQ_device": (C.c_int, [_vp, _vp, _vp, _vp]),
+        "edb_qcalc_calQ_batch_f32_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
+        "edb_qcalc_copy_B": (C.c_int, [_vp, C.c_longlong, C.c_longlong, _dp]),
+        "edb_qcalc_set_B": (C.c_int, [_vp, _dp]),
+        "edb_qcalc_get_info": (C.c_int, [_vp, C.POINTER(QCalcInfo)]),
+        "edb_fft3d_fft": (C.c_int, [C.c_int, C.c_int, C.c_int, _dp, _dp]),
+        "edb_fft3d_ifft": (C.c_int, [C.c_int, C.c_int, C.c_int, _dp, _dp]),
+        "edb_fft3d_device": (C.c_int, [C.c_int, C.c_int, _vp, _vp, C.c_int, C.c_int, _vp]),
+        "edb_efix_create": (C.c_int, [C.c_int, C.c_double, C.POINTER(_vp)]),
+        "edb_efix_destroy": (C.c_int, [_vp]),
+        "edb_efix_set_average": (C.c_int, [_vp, C.c_int, _dp]),
+        "edb_efix_entropy": (C.c_int, [_vp, C.c_int, _dp, _dp]),
+        "edb_efix_fixsol": (C.c_int, [_vp, C.c_int, _dp, C.c_double]),
+        "edb_efix_get_average": (C.c_int, [_vp, _dp, _ip]),
+        "edb_solver_create": (C.c_int, [C.POINTER(SolverDesc), C.POINTER(_vp)]),
+        "edb_solver_destroy": (C.c_int, [_vp]),
+        "edb_solver_set_initial": (C.c_int, [_vp, _dp]),
+        "edb_solver_run": (C.c_int, [_vp, C.c_double, C.c_double, C.c_double, _ip]),
+        "edb_solver_get": (C.c_int, [_vp, _dp, _dp]),
+        "edb_solver_trace": (C.c_int, [_vp, _dp, _dp, C.c_int, _ip]),
+        "edb_batch_create": (C.c_int, [_vp, C.POINTER(BatchDesc), C.POINTER(_vp)]),
+        "edb_batch_destroy": (C.c_int, [_vp]),
+        "edb_batch_load": (C.c_int, [_vp, _dp]),
+        "edb_batch_load_device": (C.c_int, [_vp, _vp, _vp]),
+        "edb_batch_step": (C.c_int, [_vp, C.c_int, _vp]),
+        "edb_batch_read": (C.c_int, [_vp, _dp, _dp]),
+        "edb_batch_moments": (C.c_int, [_vp, _dp, _dp]),
+        "edb_batch_launches_per_step": (C.c_int, [_vp, _ip]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    return L
+
+
+lib = _load()
+
+
+def check(status: int) -> None:
+    if status != EDB_OK:
+        raise EdbError(status, lib.edb_last_error().decode(errors="replace"))
+
+
+def dptr(a: np.ndarray):
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data_as(_dp)
+
+
+def devptr(x) -> int:
+    """Device address of a torch tensor, or an int address as is."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    return x.data_ptr()
+
+
+def stream_ptr(stream) -> int:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream

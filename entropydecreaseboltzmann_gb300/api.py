@@ -1,0 +1,351 @@
+"""Python mirror of the reference's classes over the C ABI of libedb.so.
+
+Names, argument meaning and call order follow the reference:
+QCalculator (CalQ/QCalculator.h:17-62), fft3d (CalQ/fft3d.h:17-49),
+EntropyFix (CalQ/EntropyFix.h:13-46) and BKW3D (CalQ/BKW.h:22-62).
+Host arrays are numpy (complex128 for c_type, float64 for r_type), N^3
+entries in FFTW order.  Device buffers are torch tensors or raw addresses.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import (INDEX_REFERENCE, R_REFERENCE, SCHEME_CFE, SCHEME_DUFORT, SCHEME_FE,
+                   SCHEME_RK2, SCHEME_RK4, SCHEME_SSP3, BatchDesc, QCalcDesc, QCalcInfo,
+                   SolverDesc, check, devptr, dptr, lib, stream_ptr)
+
+
+def kernel_launch_count() -> int:
+    """Kernels libedb.so has launched in this process (graph replays included)."""
+    return int(lib.edb_kernel_launch_count())
+
+
+def _c128(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.complex128).reshape(-1)
+    if n is not None and a.size != n:
+        raise ValueError(f"expected {n} complex entries, got {a.size}")
+    return a
+
+
+class QCalculator:
+    """QCalculator<std::complex<double>, double>(N, alpha) on the GPU.
+
+    ``L`` (box half-width in rval), ``gamma`` (real VHS exponent) and
+    ``index_mode`` generalise constants the reference hard-codes; the
+    defaults reproduce it (QCalculator.h:31-34, 176).
+    """
+
+    def __init__(self, N: int, alpha: int = 0, *, gamma: float | None = None,
+                 L: float = R_REFERENCE, filter: bool = True,
+                 index_mode: int = INDEX_REFERENCE):
+        d = QCalcDesc()
+        check(lib.edb_qcalc_desc_init(C.byref(d), int(N), int(alpha)))
+        if gamma is not None:
+            d.gamma = float(gamma)
+        d.L = float(L)
+        d.filter = int(bool(filter))
+        d.index_mode = int(index_mode)
+        self.desc = d
+        self.N = int(N)
+        self.NQ = self.N ** 3
+        h = C.c_void_p()
+        check(lib.edb_qcalc_create(C.byref(d), C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def closeFilter(self):
+        check(lib.edb_qcalc_close_filter(self._h))
+        self.desc.filter = 0
+
+    def genB(self):
+        check(lib.edb_qcalc_genB(self._h))
+
+    def calQ(self, Qout, fin):
+        """calQ(Qout, fin) (QCalculator.h:231-257): Qout <- Q-hat(fin), FP64."""
+        fin = _c128(fin, self.NQ)
+        if Qout is None:
+            Qout = np.empty(self.NQ, dtype=np.complex128)
+        if Qout.dtype != np.complex128 or not Qout.flags["C_CONTIGUOUS"] or Qout.size != self.NQ:
+            raise ValueError("Qout must be a contiguous complex128 array of N^3 entries")
+        check(lib.edb_qcalc_calQ(self._h, dptr(fin.view(np.float64)),
+                                 dptr(Qout.reshape(-1).view(np.float64))))
+        return Qout
+
+    def calQ_device(self, d_fin, d_Q, stream=None):
+        check(lib.edb_qcalc_calQ_device(self._h, devptr(d_fin), devptr(d_Q), stream_ptr(stream)))
+
+    def calQ_batch_f32(self, S, d_fin, d_Q, stream=None):
+        check(lib.edb_qcalc_calQ_batch_f32_device(self._h, int(S), devptr(d_fin), devptr(d_Q),
+                                                  stream_ptr(stream)))
+
+    def B(self, first=0, count=None):
+        total = self.NQ * self.NQ
+        count = total - first if count is None else count
+        out = np.empty(count, dtype=np.float64)
+        check(lib.edb_qcalc_copy_B(self._h, int(first), int(count), dptr(out)))
+        return out
+
+    def set_B(self, B):
+        B = np.ascontiguousarray(B, dtype=np.float64).reshape(-1)
+        if B.size != self.NQ * self.NQ:
+            raise ValueError("B must hold N^6 entries")
+        check(lib.edb_qcalc_set_B(self._h, dptr(B)))
+
+    def info(self):
+        i = QCalcInfo()
+        check(lib.edb_qcalc_get_info(self._h, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in QCalcInfo._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib.edb_qcalc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class fft3d:
+    """fft3d (CalQ/fft3d.h:17-49) on the GPU, FP64, host buffers."""
+
+    def fft(self, Nx, Ny, Nz, re, fre):
+        """fre <- unnormalised forward DFT of re (fft3d.h:25-30)."""
+        n = Nx * Ny * Nz
+        re = _c128(re, n)
+        if fre.dtype != np.complex128 or fre.size != n or not fre.flags["C_CONTIGUOUS"]:
+            raise ValueError("fre must be a contiguous complex128 array")
+        check(lib.edb_fft3d_fft(Nx, Ny, Nz, dptr(re.view(np.float64)),
+                                dptr(fre.reshape(-1).view(np.float64))))
+        return fre
+
+    def ifft(self, Nx, Ny, Nz, re, fre):
+        """re <- backward DFT of fre times 1/(Nx Ny Nz) (fft3d.h:32-48)."""
+        n = Nx * Ny * Nz
+        fre = _c128(fre, n)
+        if re.dtype != np.complex128 or re.size != n or not re.flags["C_CONTIGUOUS"]:
+            raise ValueError("re must be a contiguous complex128 array")
+        check(lib.edb_fft3d_ifft(Nx, Ny, Nz, dptr(re.reshape(-1).view(np.float64)),
+                                 dptr(fre.view(np.float64))))
+        return re
+
+    @staticmethod
+    def device(N, batch, d_in, d_out, inverse=False, fp32=False, stream=None):
+        check(lib.edb_fft3d_device(int(N), int(batch), devptr(d_in), devptr(d_out),
+                                   int(bool(inverse)), int(bool(fp32)), stream_ptr(stream)))
+
+
+class EntropyFix:
+    """EntropyFix<int, double>(Nt, eps) (CalQ/EntropyFix.h) on the GPU."""
+
+    def __init__(self, Nt: int, eps: float = 1.0e-10):
+        h = C.c_void_p()
+        check(lib.edb_efix_create(int(Nt), float(eps), C.byref(h)))
+        self._h = h
+        self.Nt = int(Nt)
+        self.eps = float(eps)
+
+    @staticmethod
+    def _args(args):
+        # (fin) or (Nf, fin) like the reference's vector / pointer overloads
+        if len(args) == 1:
+            f = args[0]
+            return len(f), f
+        return int(args[0]), args[1]
+
+    def setAverage(self, *args):
+        Nf, f = self._args(args)
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        check(lib.edb_efix_set_average(self._h, Nf, dptr(f)))
+
+    def EntropyCal(self, *args):
+        Nf, f = self._args(args)
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        H = C.c_double()
+        check(lib.edb_efix_entropy(self._h, Nf, dptr(f), C.byref(H)))
+        return H.value
+
+    def FixSol(self, *args):
+        """FixSol(fin, aim) or FixSol(Nf, fin, aim): fin is modified in place."""
+        if len(args) == 2:
+            f, aim = args
+            Nf = len(f)
+        else:
+            Nf, f, aim = args
+        if not (isinstance(f, np.ndarray) and f.dtype == np.float64 and f.flags["C_CONTIGUOUS"]):
+            raise ValueError("fin must be a contiguous float64 numpy array (modified in place)")
+        check(lib.edb_efix_fixsol(self._h, int(Nf), dptr(f), float(aim)))
+        return f
+
+    @property
+    def average(self):
+        a = C.c_double()
+        fl = C.c_int()
+        check(lib.edb_efix_get_average(self._h, C.byref(a), C.byref(fl)))
+        return a.value
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib.edb_efix_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+class BKW3D:
+    """BKW3D<c_type, r_type>(N0, R) (CalQ/BKW.h:22-62) with every integrator
+    loop (calQ stages, stage updates, ifft, entropy, fix) on the device.
+
+    The kernel table defaults to the reference's QCalculator(N0, 0): Maxwell
+    molecules, R = 6.62132 in rval, filter on, REFERENCE index mode.
+    """
+
+    def __init__(self, N0: int, R: float, *, gamma: float = 0.0, L: float = R_REFERENCE,
+                 filter: bool = True, index_mode: int = INDEX_REFERENCE):
+        self.N0 = int(N0)
+        self.R = float(R)
+        self.N3d = self.N0 ** 3
+        self.kernel = dict(gamma=float(gamma), L=float(L), filter=bool(filter),
+                           index_mode=int(index_mode))
+        self.FixEntropy = False
+        self._F0 = None
+        self.F = None
+        self.Fhat = None
+        self.entropy_raw = None
+        self.entropy_fixed = None
+        self.nsteps = 0
+
+    def setFixEntropy(self, fix: bool = True):
+        self.FixEntropy = bool(fix)
+
+    def setInitial(self, F0):
+        """Real-space initial data (N^3 complex or real); None = setInitialValue's sinusoid."""
+        self._F0 = None if F0 is None else _c128(F0, self.N3d)
+
+    def _run(self, scheme, T0, TEnd, dt, beta=1.0):
+        d = SolverDesc()
+        d.N = self.N0
+        d.R = self.R
+        d.scheme = scheme
+        d.fix_entropy = int(self.FixEntropy)
+        d.beta = float(beta)
+        d.kernel.N = self.N0
+        d.kernel.gamma = self.kernel["gamma"]
+        d.kernel.L = self.kernel["L"]
+        d.kernel.filter = int(self.kernel["filter"])
+        d.kernel.index_mode = self.kernel["index_mode"]
+        h = C.c_void_p()
+        check(lib.edb_solver_create(C.byref(d), C.byref(h)))
+        try:
+            F0p = None if self._F0 is None else dptr(self._F0.view(np.float64))
+            check(lib.edb_solver_set_initial(h, F0p))
+            ns = C.c_int()
+            check(lib.edb_solver_run(h, float(T0), float(TEnd), float(dt), C.byref(ns)))
+            self.nsteps = ns.value
+            self.Fhat = np.empty(self.N3d, dtype=np.complex128)
+            self.F = np.empty(self.N3d, dtype=np.complex128)
+            check(lib.edb_solver_get(h, dptr(self.Fhat.view(np.float64)),
+                                     dptr(self.F.view(np.float64))))
+            raw = np.empty(ns.value)
+            fixed = np.empty(ns.value)
+            n = C.c_int()
+            check(lib.edb_solver_trace(h, dptr(raw), dptr(fixed), ns.value, C.byref(n)))
+            self.entropy_raw, self.entropy_fixed = raw, fixed
+        finally:
+            lib.edb_solver_destroy(h)
+        return self
+
+    def FEuler(self, T0, TEnd, dt):
+        return self._run(SCHEME_FE, T0, TEnd, dt)
+
+    def CFE(self, T0, TEnd, dt, beta):
+        return self._run(SCHEME_CFE, T0, TEnd, dt, beta)
+
+    def RK2(self, T0, TEnd, dt):
+        return self._run(SCHEME_RK2, T0, TEnd, dt)
+
+    def SSP3(self, T0, TEnd, dt):
+        return self._run(SCHEME_SSP3, T0, TEnd, dt)
+
+    def RK4(self, T0, TEnd, dt):
+        return self._run(SCHEME_RK4, T0, TEnd, dt)
+
+    def DUFORT(self, T0, TEnd, dt, beta):
+        return self._run(SCHEME_DUFORT, T0, TEnd, dt, beta)
+
+
+class BatchSolver:
+    """S independent solves sharing one ALIASED kernel table.
+
+    Q-hat runs in complex FP32 with compensated sums (edb_qcalc_calQ_batch_f32_device);
+    the RK state, stage updates, inverse transforms, moments and the entropy
+    rule run in FP64.  One CUDA graph launch advances every solve by one step.
+    """
+
+    def __init__(self, qcalc: QCalculator, S: int, R: float, scheme: int = SCHEME_RK4,
+                 dt: float = 0.01, fix_entropy: bool = False):
+        d = BatchDesc()
+        d.S = int(S)
+        d.N = qcalc.N
+        d.R = float(R)
+        d.scheme = int(scheme)
+        d.dt = float(dt)
+        d.fix_entropy = int(bool(fix_entropy))
+        h = C.c_void_p()
+        check(lib.edb_batch_create(qcalc.handle, C.byref(d), C.byref(h)))
+        self._h = h
+        self.q = qcalc
+        self.S = int(S)
+        self.N = qcalc.N
+        self.NQ = self.N ** 3
+
+    def load(self, F0_real):
+        F0 = np.ascontiguousarray(F0_real, dtype=np.float64).reshape(-1)
+        if F0.size != self.S * self.NQ:
+            raise ValueError("expected S x N^3 real values")
+        check(lib.edb_batch_load(self._h, dptr(F0)))
+
+    def load_device(self, d_F0_real, stream=None):
+        check(lib.edb_batch_load_device(self._h, devptr(d_F0_real), stream_ptr(stream)))
+
+    def step(self, nsteps=1, stream=None):
+        check(lib.edb_batch_step(self._h, int(nsteps), stream_ptr(stream)))
+
+    def read(self, real=True, fhat=False):
+        F = np.empty(self.S * self.NQ) if real else None
+        Fh = np.empty(self.S * self.NQ, dtype=np.complex128) if fhat else None
+        check(lib.edb_batch_read(self._h, None if F is None else dptr(F),
+                                 None if Fh is None else dptr(Fh.view(np.float64))))
+        out = []
+        if real:
+            out.append(F.reshape(self.S, self.NQ))
+        if fhat:
+            out.append(Fh.reshape(self.S, self.NQ))
+        return out[0] if len(out) == 1 else tuple(out)
+
+    def moments(self):
+        m = np.empty(self.S * 5)
+        H = np.empty(self.S)
+        check(lib.edb_batch_moments(self._h, dptr(m), dptr(H)))
+        return m.reshape(self.S, 5), H
+
+    def launches_per_step(self):
+        n = C.c_int()
+        check(lib.edb_batch_launches_per_step(self._h, C.byref(n)))
+        return n.value
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib.edb_batch_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass

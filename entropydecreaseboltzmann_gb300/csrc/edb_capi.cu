@@ -1,0 +1,906 @@
+// C ABI of libedb.so (declared in include/edb.h): handles, host/device entry
+// points, the device-resident BKW3D integrator and the batched solver.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "edb_internal.cuh"
+
+namespace edb {
+
+static thread_local std::string g_err;
+static std::atomic<long long> g_launches{0};
+
+void set_error(const std::string &msg) { g_err = msg; }
+edb_status fail(edb_status s, const std::string &msg) {
+  g_err = msg;
+  return s;
+}
+edb_status cuda_fail(cudaError_t e, const char *what) {
+  g_err = std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e);
+  return EDB_ECUDA;
+}
+void count_launch(int n) { g_launches += n; }
+
+edb_status ensure_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    return fail(EDB_ECUDA, std::string("no usable CUDA device: ") +
+                               (e != cudaSuccess ? cudaGetErrorString(e) : "device count 0"));
+  return EDB_OK;
+}
+
+template <typename T>
+static edb_status dalloc(T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return EDB_OK;
+  cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(EDB_ENOMEM, std::string("cudaMalloc of ") + std::to_string(count * sizeof(T)) +
+                                " bytes failed: " + cudaGetErrorString(e));
+  }
+  return EDB_OK;
+}
+template <typename T>
+static void dfree(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+}  // namespace edb
+
+using namespace edb;
+
+// ====================================================================== misc
+
+extern "C" const char *edb_last_error(void) { return g_err.c_str(); }
+
+extern "C" const char *edb_status_string(edb_status s) {
+  switch (s) {
+    case EDB_OK: return "EDB_OK";
+    case EDB_EINVAL: return "EDB_EINVAL";
+    case EDB_ENOMEM: return "EDB_ENOMEM";
+    case EDB_ECUDA: return "EDB_ECUDA";
+    case EDB_ETIMEDOUT: return "EDB_ETIMEDOUT";
+    case EDB_ENOTREADY: return "EDB_ENOTREADY";
+    case EDB_EBUSY: return "EDB_EBUSY";
+    case EDB_ENOTFOUND: return "EDB_ENOTFOUND";
+  }
+  return "EDB_UNKNOWN";
+}
+
+extern "C" int edb_version(void) { return 100; }
+extern "C" long long edb_kernel_launch_count(void) { return g_launches.load(); }
+
+// =============================================================== QCalculator
+
+struct edb_qcalc {
+  edb_qcalc_desc d;
+  QParams p;
+  cudaStream_t st = nullptr;
+  double *B64 = nullptr;    // [l][k] centred, N^3 x KC... stored N^3 x N^3
+  float *B32 = nullptr;     // FFTW order [l][k] (ALIASED only)
+  double2 *partial = nullptr;
+  double2 *fin = nullptr, *Q = nullptr;  // host-API staging
+  int nchunk = 0;
+  bool ready = false;
+};
+
+static edb_status check_desc(const edb_qcalc_desc *d) {
+  if (!d) return fail(EDB_EINVAL, "null descriptor");
+  if (d->N < 3 || d->N > 64) return fail(EDB_EINVAL, "N must be in [3, 64]");
+  if (!(d->gamma >= 0.0 && d->gamma <= 2.0)) return fail(EDB_EINVAL, "gamma must be in [0, 2]");
+  if (!(d->L > 0.0)) return fail(EDB_EINVAL, "L must be positive");
+  if (d->index_mode != EDB_INDEX_REFERENCE && d->index_mode != EDB_INDEX_ALIASED)
+    return fail(EDB_EINVAL, "unknown index mode");
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_qcalc_desc_init(edb_qcalc_desc *d, int N, int alpha) {
+  if (!d) return fail(EDB_EINVAL, "null descriptor");
+  d->N = N;
+  d->gamma = (double)alpha;
+  d->L = EDB_R_REFERENCE;
+  d->filter = 1;
+  d->index_mode = EDB_INDEX_REFERENCE;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_qcalc_create(const edb_qcalc_desc *d, edb_qcalc **out) {
+  if (!out) return fail(EDB_EINVAL, "null output pointer");
+  *out = nullptr;
+  EDB_TRY(check_desc(d));
+  EDB_TRY(ensure_device());
+  edb_qcalc *q = new edb_qcalc();
+  q->d = *d;
+  q->p = make_qparams(d->N, d->index_mode);
+  cudaError_t e = cudaStreamCreateWithFlags(&q->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete q;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  *out = q;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_qcalc_destroy(edb_qcalc *q) {
+  if (!q) return EDB_OK;
+  if (q->st) cudaStreamSynchronize(q->st);
+  dfree(q->B64);
+  dfree(q->B32);
+  dfree(q->partial);
+  dfree(q->fin);
+  dfree(q->Q);
+  if (q->st) cudaStreamDestroy(q->st);
+  delete q;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_qcalc_close_filter(edb_qcalc *q) {
+  if (!q) return fail(EDB_EINVAL, "null handle");
+  q->d.filter = 0;
+  return EDB_OK;
+}
+
+static int amax_of(int N) {
+  int n = (N - 1) / 2;
+  int hi = 2 * (N - 1 - n);
+  if (N - 1 > hi) hi = N - 1;
+  return 3 * hi * hi;
+}
+
+static edb_status qcalc_alloc_work(edb_qcalc *q) {
+  if (!q->partial) {
+    q->nchunk = calq64_nchunk(q->p);
+    EDB_TRY(dalloc(&q->partial, (size_t)q->nchunk * q->p.KC));
+  }
+  if (!q->fin) EDB_TRY(dalloc(&q->fin, (size_t)q->p.NQ));
+  if (!q->Q) EDB_TRY(dalloc(&q->Q, (size_t)q->p.NQ));
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_qcalc_genB(edb_qcalc *q) {
+  if (!q) return fail(EDB_EINVAL, "null handle");
+  const int N = q->d.N;
+  const long long NQ = q->p.NQ;
+  const int amax = amax_of(N);
+  double *T = nullptr, *sigma = nullptr, *Bmm = nullptr;
+  edb_status s = EDB_OK;
+  if (!q->B64) EDB_TRY(dalloc(&q->B64, (size_t)NQ * NQ));
+  if (q->d.index_mode == EDB_INDEX_ALIASED && !q->B32)
+    EDB_TRY(dalloc(&q->B32, (size_t)NQ * NQ + 64));  // +64: masked tail reads of calq32
+  EDB_TRY(qcalc_alloc_work(q));
+  s = dalloc(&T, (size_t)(amax + 1) * (amax + 1));
+  if (s == EDB_OK) s = dalloc(&sigma, 64);
+  if (s == EDB_OK) s = dalloc(&Bmm, (size_t)NQ);
+  if (s == EDB_OK) s = launch_ftable(N, q->d.gamma, T, amax, q->st);
+  if (s == EDB_OK)
+    s = launch_bmm(N, q->d.gamma, q->d.L, q->d.filter, q->d.index_mode, T, amax, sigma, Bmm,
+                   q->st);
+  if (s == EDB_OK)
+    s = launch_genB(N, q->d.gamma, q->d.L, q->d.filter, q->d.index_mode, T, amax, sigma, Bmm,
+                    q->B64, q->B32, q->st);
+  cudaError_t e = cudaStreamSynchronize(q->st);
+  dfree(T);
+  dfree(sigma);
+  dfree(Bmm);
+  if (s != EDB_OK) return s;
+  if (e != cudaSuccess) return cuda_fail(e, "genB");
+  q->ready = true;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_qcalc_set_B(edb_qcalc *q, const double *host_B) {
+  if (!q || !host_B) return fail(EDB_EINVAL, "null argument");
+  const long long NQ = q->p.NQ;
+  if (!q->B64) EDB_TRY(dalloc(&q->B64, (size_t)NQ * NQ));
+  EDB_TRY(qcalc_alloc_work(q));
+  EDB_CUDA(cudaMemcpy(q->B64, host_B, sizeof(double) * NQ * NQ, cudaMemcpyHostToDevice));
+  dfree(q->B32);  // the FP32 copy no longer matches
+  q->ready = true;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_qcalc_copy_B(edb_qcalc *q, long long first, long long count,
+                                       double *host_out) {
+  if (!q || !host_out) return fail(EDB_EINVAL, "null argument");
+  if (!q->ready) return fail(EDB_ENOTREADY, "genB has not run");
+  const long long total = q->p.NQ * q->p.NQ;
+  if (first < 0 || count < 0 || first + count > total) return fail(EDB_EINVAL, "range out of table");
+  EDB_CUDA(cudaMemcpy(host_out, q->B64 + first, sizeof(double) * count, cudaMemcpyDeviceToHost));
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_qcalc_get_info(edb_qcalc *q, edb_qcalc_info *out) {
+  if (!q || !out) return fail(EDB_EINVAL, "null argument");
+  out->N = q->p.N;
+  out->n = q->p.n;
+  out->P = q->p.P;
+  out->NQ = q->p.NQ;
+  out->terms = q->p.NQ * q->p.KC;
+  out->B_bytes = q->p.NQ * q->p.NQ * (long long)sizeof(double);
+  out->has_B32 = q->B32 != nullptr;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_qcalc_calQ_device(edb_qcalc *q, const double *d_fin, double *d_Qout,
+                                            void *stream) {
+  if (!q || !d_fin || !d_Qout) return fail(EDB_EINVAL, "null argument");
+  if (!q->ready) return fail(EDB_ENOTREADY, "calQ before genB");
+  return launch_calq64(q->p, q->B64, (const double2 *)d_fin, q->partial, (double2 *)d_Qout,
+                       (cudaStream_t)stream);
+}
+
+extern "C" edb_status edb_qcalc_calQ(edb_qcalc *q, const double *fin, double *Qout) {
+  if (!q || !fin || !Qout) return fail(EDB_EINVAL, "null argument");
+  if (!q->ready) return fail(EDB_ENOTREADY, "calQ before genB");
+  const size_t bytes = sizeof(double2) * q->p.NQ;
+  EDB_CUDA(cudaMemcpyAsync(q->fin, fin, bytes, cudaMemcpyHostToDevice, q->st));
+  EDB_TRY(launch_calq64(q->p, q->B64, q->fin, q->partial, q->Q, q->st));
+  EDB_CUDA(cudaMemcpyAsync(Qout, q->Q, bytes, cudaMemcpyDeviceToHost, q->st));
+  EDB_CUDA(cudaStreamSynchronize(q->st));
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_qcalc_calQ_batch_f32_device(edb_qcalc *q, int S, const float *d_fin,
+                                                      float *d_Qout, void *stream) {
+  if (!q || !d_fin || !d_Qout) return fail(EDB_EINVAL, "null argument");
+  if (S < 1) return fail(EDB_EINVAL, "S must be positive");
+  if (q->d.index_mode != EDB_INDEX_ALIASED)
+    return fail(EDB_EINVAL, "the batched path runs the ALIASED index mode");
+  if (!q->ready || !q->B32) return fail(EDB_ENOTREADY, "batched calQ before genB");
+  return launch_calq32_batch(q->d.N, S, q->B32, (const float2 *)d_fin, (float2 *)d_Qout,
+                             (cudaStream_t)stream);
+}
+
+// ===================================================================== fft3d
+
+static edb_status fft_host(int nx, int ny, int nz, const double *in, double *out, int inverse) {
+  if (!in || !out) return fail(EDB_EINVAL, "null argument");
+  if (nx != ny || ny != nz) return fail(EDB_EINVAL, "fft3d: cubes only (fft3d.h:43)");
+  EDB_TRY(ensure_device());
+  const int N = nx;
+  const size_t bytes = sizeof(double2) * (size_t)N * N * N;
+  double2 *a = nullptr, *b = nullptr;
+  EDB_TRY(dalloc(&a, (size_t)N * N * N));
+  edb_status s = dalloc(&b, (size_t)N * N * N);
+  if (s == EDB_OK) {
+    cudaError_t e = cudaMemcpy(a, in, bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) s = cuda_fail(e, "cudaMemcpy");
+  }
+  if (s == EDB_OK) s = launch_dft3d(N, 1, a, b, nullptr, inverse, 0, 0);
+  if (s == EDB_OK) {
+    cudaError_t e = cudaMemcpy(out, b, bytes, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) s = cuda_fail(e, "cudaMemcpy");
+  }
+  dfree(a);
+  dfree(b);
+  return s;
+}
+
+extern "C" edb_status edb_fft3d_fft(int nx, int ny, int nz, const double *re, double *fre) {
+  return fft_host(nx, ny, nz, re, fre, 0);
+}
+extern "C" edb_status edb_fft3d_ifft(int nx, int ny, int nz, double *re, const double *fre) {
+  return fft_host(nx, ny, nz, fre, re, 1);
+}
+extern "C" edb_status edb_fft3d_device(int N, int batch, const void *d_in, void *d_out,
+                                       int inverse, int fp32, void *stream) {
+  if (!d_in || !d_out || batch < 1) return fail(EDB_EINVAL, "bad argument");
+  return launch_dft3d(N, batch, d_in, d_out, nullptr, inverse, fp32, (cudaStream_t)stream);
+}
+
+// ================================================================ EntropyFix
+
+struct edb_efix {
+  int Nt;
+  double eps;
+  EfixState *st = nullptr;
+  double *f = nullptr, *H = nullptr;
+};
+
+extern "C" edb_status edb_efix_create(int Nt, double eps, edb_efix **out) {
+  if (!out) return fail(EDB_EINVAL, "null output pointer");
+  *out = nullptr;
+  if (Nt < 1) return fail(EDB_EINVAL, "Nt must be positive");
+  EDB_TRY(ensure_device());
+  edb_efix *e = new edb_efix();
+  e->Nt = Nt;
+  e->eps = eps;
+  edb_status s = dalloc(&e->st, 1);
+  if (s == EDB_OK) s = dalloc(&e->f, (size_t)Nt);
+  if (s == EDB_OK) s = dalloc(&e->H, 1);
+  if (s == EDB_OK) {
+    EfixState init = {1.0, 0, 0, 1.0, 0, 0};  // Averagef = 1.0, flag false (EntropyFix.h:20-22)
+    cudaError_t ce = cudaMemcpy(e->st, &init, sizeof(init), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) s = cuda_fail(ce, "cudaMemcpy");
+  }
+  if (s != EDB_OK) {
+    dfree(e->st);
+    dfree(e->f);
+    dfree(e->H);
+    delete e;
+    return s;
+  }
+  *out = e;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_efix_destroy(edb_efix *e) {
+  if (!e) return EDB_OK;
+  dfree(e->st);
+  dfree(e->f);
+  dfree(e->H);
+  delete e;
+  return EDB_OK;
+}
+
+static edb_status efix_check(edb_efix *e, int Nf, const double *f) {
+  if (!e || !f) return fail(EDB_EINVAL, "null argument");
+  // the reference asserts Nf == Nt (EntropyFix.h:124, 183, 270)
+  if (Nf != e->Nt) return fail(EDB_EINVAL, "Nf must equal Nt");
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_efix_set_average(edb_efix *e, int Nf, const double *f) {
+  EDB_TRY(efix_check(e, Nf, f));
+  EDB_CUDA(cudaMemcpy(e->f, f, sizeof(double) * Nf, cudaMemcpyHostToDevice));
+  EDB_TRY(launch_efix_average(Nf, e->f, e->st, 0));
+  EDB_CUDA(cudaDeviceSynchronize());
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_efix_entropy(edb_efix *e, int Nf, const double *f, double *H) {
+  EDB_TRY(efix_check(e, Nf, f));
+  if (!H) return fail(EDB_EINVAL, "null output");
+  EDB_CUDA(cudaMemcpy(e->f, f, sizeof(double) * Nf, cudaMemcpyHostToDevice));
+  EDB_TRY(launch_efix_entropy(Nf, e->f, e->st, e->eps, e->H, 0));
+  EDB_CUDA(cudaMemcpy(H, e->H, sizeof(double), cudaMemcpyDeviceToHost));
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_efix_fixsol(edb_efix *e, int Nf, double *f, double aim) {
+  EDB_TRY(efix_check(e, Nf, f));
+  EDB_CUDA(cudaMemcpy(e->f, f, sizeof(double) * Nf, cudaMemcpyHostToDevice));
+  EDB_TRY(launch_efix_fixsol(Nf, e->f, e->st, e->eps, aim, 0));
+  EDB_CUDA(cudaMemcpy(f, e->f, sizeof(double) * Nf, cudaMemcpyDeviceToHost));
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_efix_get_average(edb_efix *e, double *avg, int *latched) {
+  if (!e) return fail(EDB_EINVAL, "null handle");
+  EfixState h;
+  EDB_CUDA(cudaMemcpy(&h, e->st, sizeof(h), cudaMemcpyDeviceToHost));
+  if (avg) *avg = h.avg;
+  if (latched) *latched = h.avg_flag;
+  return EDB_OK;
+}
+
+// ================================================================ integrator
+
+struct edb_solver {
+  edb_solver_desc d;
+  edb_qcalc *q = nullptr;
+  cudaStream_t st = nullptr;
+  long long NQ = 0;
+  double2 *F = nullptr, *Fhat = nullptr, *Fold = nullptr;
+  double2 *Qs[4] = {nullptr, nullptr, nullptr, nullptr};
+  double2 *Fs[3] = {nullptr, nullptr, nullptr};
+  EfixState *state = nullptr;
+  double *tr_raw = nullptr, *tr_fixed = nullptr;
+  int trace_cap = 0, trace_n = 0;
+  bool has_initial = false;
+  std::vector<double> F0;
+};
+
+extern "C" edb_status edb_solver_create(const edb_solver_desc *d, edb_solver **out) {
+  if (!d || !out) return fail(EDB_EINVAL, "null argument");
+  *out = nullptr;
+  if (d->scheme < EDB_SCHEME_FE || d->scheme > EDB_SCHEME_DUFORT)
+    return fail(EDB_EINVAL, "unknown scheme");
+  if (d->kernel.N != d->N) return fail(EDB_EINVAL, "kernel.N must equal N");
+  if (!(d->R > 0)) return fail(EDB_EINVAL, "R must be positive");
+  edb_solver *s = new edb_solver();
+  s->d = *d;
+  s->NQ = (long long)d->N * d->N * d->N;
+  edb_status rc = edb_qcalc_create(&d->kernel, &s->q);
+  if (rc == EDB_OK) rc = edb_qcalc_genB(s->q);
+  if (rc == EDB_OK) {
+    cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamCreate");
+  }
+  const size_t NQ = (size_t)s->NQ;
+  if (rc == EDB_OK) rc = dalloc(&s->F, NQ);
+  if (rc == EDB_OK) rc = dalloc(&s->Fhat, NQ);
+  if (rc == EDB_OK) rc = dalloc(&s->Fold, NQ);
+  for (int i = 0; i < 4 && rc == EDB_OK; ++i) rc = dalloc(&s->Qs[i], NQ);
+  for (int i = 0; i < 3 && rc == EDB_OK; ++i) rc = dalloc(&s->Fs[i], NQ);
+  if (rc == EDB_OK) rc = dalloc(&s->state, 1);
+  if (rc != EDB_OK) {
+    edb_solver_destroy(s);
+    return rc;
+  }
+  *out = s;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_solver_destroy(edb_solver *s) {
+  if (!s) return EDB_OK;
+  if (s->st) cudaStreamSynchronize(s->st);
+  dfree(s->F);
+  dfree(s->Fhat);
+  dfree(s->Fold);
+  for (auto &p : s->Qs) dfree(p);
+  for (auto &p : s->Fs) dfree(p);
+  dfree(s->state);
+  dfree(s->tr_raw);
+  dfree(s->tr_fixed);
+  if (s->q) edb_qcalc_destroy(s->q);
+  if (s->st) cudaStreamDestroy(s->st);
+  delete s;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_solver_set_initial(edb_solver *s, const double *F0) {
+  if (!s) return fail(EDB_EINVAL, "null handle");
+  if (F0)
+    s->F0.assign(F0, F0 + 2 * s->NQ);
+  else
+    s->F0.clear();
+  s->has_initial = true;
+  return EDB_OK;
+}
+
+// Step counts of `do { t += dt; ... } while (t < TEnd)` with the reference's
+// floating accumulation (BKW.h:218-248); DUFORT adds 8 RK2 start-up steps
+// that advance t by dt/8 (:547-587).
+static int count_steps(int scheme, double T0, double TEnd, double dt) {
+  double t = T0;
+  int n = 0;
+  if (scheme == EDB_SCHEME_DUFORT) {
+    for (int i = 0; i < 8; ++i) t += dt / 8;
+    n = 8;
+  }
+  do {
+    t += dt;
+    ++n;
+  } while (t < TEnd && n < 100000000);
+  return n;
+}
+
+// One step of the chosen scheme on the device (the loop bodies of BKW.h).
+static edb_status solver_step(edb_solver *s, double dt, bool dufort_startup) {
+  const long long n = s->NQ;
+  cudaStream_t st = s->st;
+  edb_qcalc *q = s->q;
+  double2 *Fh = s->Fhat, **Q = s->Qs, **F = s->Fs;
+  auto calq = [&](const double2 *in, double2 *out) {
+    return launch_calq64(q->p, q->B64, in, q->partial, out, st);
+  };
+  switch (s->d.scheme) {
+    case EDB_SCHEME_FE:  // BKW.h:220-222
+      EDB_TRY(calq(Fh, Q[0]));
+      EDB_TRY(launch_stage(n, STAGE_AXPY, 0, dt, 0, Fh, Fh, 0, 0, Q[0], 0, 0, 0, 0, st));
+      break;
+    case EDB_SCHEME_CFE: {  // BKW.h:281-283
+      const double beta = s->d.beta;
+      EDB_TRY(calq(Fh, Q[0]));
+      EDB_TRY(launch_stage(n, STAGE_AXPY, 0, (1. - exp(-beta * dt)) / beta, 0, Fh, Fh, 0, 0, Q[0],
+                           0, 0, 0, 0, st));
+      break;
+    }
+    case EDB_SCHEME_RK2:  // BKW.h:341-346
+      EDB_TRY(calq(Fh, Q[0]));
+      EDB_TRY(launch_stage(n, STAGE_AXPY, 0, 0.5 * dt, 0, F[0], Fh, 0, 0, Q[0], 0, 0, 0, 0, st));
+      EDB_TRY(calq(F[0], Q[0]));
+      EDB_TRY(launch_stage(n, STAGE_AXPY, 0, dt, 0, Fh, Fh, 0, 0, Q[0], 0, 0, 0, 0, st));
+      break;
+    case EDB_SCHEME_SSP3:  // BKW.h:416-424
+      EDB_TRY(calq(Fh, Q[0]));
+      EDB_TRY(launch_stage(n, STAGE_AXPY, 0, dt, 0, F[0], Fh, 0, 0, Q[0], 0, 0, 0, 0, st));
+      EDB_TRY(calq(F[0], Q[0]));
+      EDB_TRY(launch_stage(n, STAGE_SSP3_2, 0, 0.25 * dt, 0, F[1], Fh, F[0], 0, Q[0], 0, 0, 0, 0,
+                           st));
+      EDB_TRY(calq(F[1], Q[0]));
+      EDB_TRY(launch_stage(n, STAGE_SSP3_3, 0, 2. / 3. * dt, 0, Fh, Fh, F[1], 0, Q[0], 0, 0, 0, 0,
+                           st));
+      break;
+    case EDB_SCHEME_RK4:  // BKW.h:482-494
+      EDB_TRY(calq(Fh, Q[0]));
+      EDB_TRY(launch_stage(n, STAGE_AXPY, 0, 0.5 * dt, 0, F[0], Fh, 0, 0, Q[0], 0, 0, 0, 0, st));
+      EDB_TRY(calq(F[0], Q[1]));
+      EDB_TRY(launch_stage(n, STAGE_AXPY, 0, 0.5 * dt, 0, F[1], Fh, 0, 0, Q[1], 0, 0, 0, 0, st));
+      EDB_TRY(calq(F[1], Q[2]));
+      EDB_TRY(launch_stage(n, STAGE_AXPY, 0, dt, 0, F[2], Fh, 0, 0, Q[2], 0, 0, 0, 0, st));
+      EDB_TRY(calq(F[2], Q[3]));
+      EDB_TRY(launch_stage(n, STAGE_RK4, 0, dt / 6., 0, Fh, Fh, 0, 0, Q[0], Q[1], Q[2], Q[3], 0,
+                           st));
+      break;
+    case EDB_SCHEME_DUFORT:
+      if (dufort_startup) {  // BKW.h:551-556 (updates use dt, not dt/8)
+        EDB_TRY(calq(Fh, Q[0]));
+        EDB_TRY(
+            launch_stage(n, STAGE_AXPY, 0, 0.5 * dt, 0, F[0], Fh, 0, 0, Q[0], 0, 0, 0, 0, st));
+        EDB_TRY(calq(F[0], Q[0]));
+        EDB_TRY(launch_stage(n, STAGE_AXPY, 0, dt, 0, Fh, Fh, 0, 0, Q[0], 0, 0, 0, 0, st));
+      } else {  // BKW.h:595-598, then F_old = F1 (:630)
+        const double beta = s->d.beta;
+        EDB_TRY(calq(Fh, Q[0]));
+        EDB_CUDA(cudaMemcpyAsync(F[0], Fh, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+        EDB_TRY(launch_stage(n, STAGE_DUFORT, 1. / (1. + beta * dt), dt, beta * dt, Fh, 0, F[0],
+                             s->Fold, Q[0], 0, 0, 0, 0, st));
+      }
+      break;
+  }
+  // fft3(isInverse) then calEntropy and the fix rule
+  EDB_TRY(launch_dft3d(s->d.N, 1, Fh, s->F, nullptr, 1, 0, st));
+  int fix_mode = 0;
+  if (s->d.scheme == EDB_SCHEME_FE) fix_mode = s->d.fix_entropy ? 1 : 0;
+  else if (s->d.scheme == EDB_SCHEME_CFE) fix_mode = s->d.fix_entropy ? 2 : 0;
+  else if (s->d.scheme == EDB_SCHEME_SSP3 || s->d.scheme == EDB_SCHEME_RK4) fix_mode = 2;
+  EDB_TRY(launch_step_entropy(s->d.N, 1, s->d.R, s->F, s->state, 1.0e-10, fix_mode, s->tr_raw,
+                              s->tr_fixed, s->trace_cap, st));
+  if (s->d.scheme == EDB_SCHEME_DUFORT && !dufort_startup)
+    EDB_CUDA(cudaMemcpyAsync(s->Fold, F[0], sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_solver_run(edb_solver *s, double T0, double TEnd, double dt,
+                                     int *nsteps) {
+  if (!s) return fail(EDB_EINVAL, "null handle");
+  if (!(dt > 0)) return fail(EDB_EINVAL, "dt must be positive");
+  const int total = count_steps(s->d.scheme, T0, TEnd, dt);
+  const long long n = s->NQ;
+  cudaStream_t st = s->st;
+  dfree(s->tr_raw);
+  dfree(s->tr_fixed);
+  s->trace_cap = total;
+  EDB_TRY(dalloc(&s->tr_raw, (size_t)total));
+  EDB_TRY(dalloc(&s->tr_fixed, (size_t)total));
+  // initial data -> F, Fhat = fft(F) (BKW.h:197-198)
+  if (s->has_initial && !s->F0.empty())
+    EDB_CUDA(cudaMemcpyAsync(s->F, s->F0.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, st));
+  else
+    EDB_TRY(launch_sinusoid_init(s->d.N, s->d.R, s->F, st));
+  EDB_TRY(launch_dft3d(s->d.N, 1, s->F, s->Fhat, nullptr, 0, 0, st));
+  if (s->d.scheme == EDB_SCHEME_DUFORT)
+    EDB_CUDA(cudaMemcpyAsync(s->Fold, s->Fhat, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+  // entropy0 and the step counter: FE starts from calEntropy() and step 1
+  // (BKW.h:214-216); the others from 1. and step 0.
+  EfixState init = {1.0, 0, 0, 1.0, 0, 0};
+  EDB_CUDA(cudaMemcpyAsync(s->state, &init, sizeof(init), cudaMemcpyHostToDevice, st));
+  if (s->d.scheme == EDB_SCHEME_FE) {
+    EDB_TRY(launch_calentropy(s->d.N, 1, s->d.R, s->F, &s->state->H_prev, st));
+    int one = 1;
+    EDB_CUDA(cudaMemcpyAsync(&s->state->step, &one, sizeof(int), cudaMemcpyHostToDevice, st));
+  }
+  EDB_CUDA(cudaStreamSynchronize(st));
+  int done = 0;
+  if (s->d.scheme == EDB_SCHEME_DUFORT) {
+    for (int i = 0; i < 8; ++i, ++done) EDB_TRY(solver_step(s, dt, true));
+    // step counter restarts at 0 (BKW.h:592); it gates no fix for DUFORT
+  }
+  // The steady-state step is captured once as a CUDA graph and replayed.
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  const int remaining = total - done;
+  if (remaining > 0) {
+    EDB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    edb_status rc = solver_step(s, dt, false);
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (rc != EDB_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    for (int i = 0; i < remaining; ++i) {
+      e = cudaGraphLaunch(exec, st);
+      if (e != cudaSuccess) break;
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
+  }
+  EDB_CUDA(cudaStreamSynchronize(st));
+  s->trace_n = total;
+  if (nsteps) *nsteps = total;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_solver_get(edb_solver *s, double *Fhat, double *F) {
+  if (!s) return fail(EDB_EINVAL, "null handle");
+  const size_t bytes = sizeof(double2) * s->NQ;
+  if (Fhat) EDB_CUDA(cudaMemcpy(Fhat, s->Fhat, bytes, cudaMemcpyDeviceToHost));
+  if (F) EDB_CUDA(cudaMemcpy(F, s->F, bytes, cudaMemcpyDeviceToHost));
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_solver_trace(edb_solver *s, double *raw, double *fixed, int cap, int *n) {
+  if (!s) return fail(EDB_EINVAL, "null handle");
+  int k = s->trace_n < cap ? s->trace_n : cap;
+  if (k > 0 && raw) EDB_CUDA(cudaMemcpy(raw, s->tr_raw, sizeof(double) * k, cudaMemcpyDeviceToHost));
+  if (k > 0 && fixed)
+    EDB_CUDA(cudaMemcpy(fixed, s->tr_fixed, sizeof(double) * k, cudaMemcpyDeviceToHost));
+  if (n) *n = s->trace_n;
+  return EDB_OK;
+}
+
+// ============================================================ batched solves
+
+struct edb_batch {
+  edb_batch_desc d;
+  edb_qcalc *q = nullptr;
+  cudaStream_t st = nullptr;  // internal stream used when the caller passes NULL
+  long long NQ = 0, n = 0;    // N^3, S*N^3
+  double2 *Fhat = nullptr, *F = nullptr;
+  double2 *Fs[3] = {nullptr, nullptr, nullptr};
+  float2 *Qs[4] = {nullptr, nullptr, nullptr, nullptr};
+  float2 *in32 = nullptr;
+  EfixState *state = nullptr;
+  double *tr_raw = nullptr, *tr_fixed = nullptr;
+  double *mom = nullptr, *H = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t exec_stream = nullptr;
+  int launches_per_step = 0;
+};
+
+extern "C" edb_status edb_batch_create(edb_qcalc *q, const edb_batch_desc *d, edb_batch **out) {
+  if (!q || !d || !out) return fail(EDB_EINVAL, "null argument");
+  *out = nullptr;
+  if (d->S < 1) return fail(EDB_EINVAL, "S must be positive");
+  if (d->N != q->d.N) return fail(EDB_EINVAL, "batch N differs from the kernel table's N");
+  if (d->scheme != EDB_SCHEME_FE && d->scheme != EDB_SCHEME_SSP3 && d->scheme != EDB_SCHEME_RK4)
+    return fail(EDB_EINVAL, "batched schemes: FE, SSP3, RK4");
+  if (q->d.index_mode != EDB_INDEX_ALIASED || !q->B32)
+    return fail(EDB_ENOTREADY, "batched solves need an ALIASED table after genB");
+  edb_batch *b = new edb_batch();
+  b->d = *d;
+  b->q = q;
+  b->NQ = (long long)d->N * d->N * d->N;
+  b->n = b->NQ * d->S;
+  const size_t n = (size_t)b->n;
+  edb_status rc = EDB_OK;
+  cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamCreate");
+  if (rc == EDB_OK) rc = dalloc(&b->Fhat, n);
+  if (rc == EDB_OK) rc = dalloc(&b->F, n);
+  const int nstage = d->scheme == EDB_SCHEME_RK4 ? 3 : (d->scheme == EDB_SCHEME_SSP3 ? 2 : 0);
+  const int nq = d->scheme == EDB_SCHEME_RK4 ? 4 : 1;
+  for (int i = 0; i < nstage && rc == EDB_OK; ++i) rc = dalloc(&b->Fs[i], n);
+  for (int i = 0; i < nq && rc == EDB_OK; ++i) rc = dalloc(&b->Qs[i], n);
+  if (rc == EDB_OK) rc = dalloc(&b->in32, n);
+  if (rc == EDB_OK) rc = dalloc(&b->state, (size_t)d->S);
+  if (rc == EDB_OK) rc = dalloc(&b->mom, (size_t)d->S * 5);
+  if (rc == EDB_OK) rc = dalloc(&b->H, (size_t)d->S);
+  if (rc == EDB_OK) rc = dalloc(&b->tr_raw, (size_t)d->S);
+  if (rc == EDB_OK) rc = dalloc(&b->tr_fixed, (size_t)d->S);
+  if (rc != EDB_OK) {
+    edb_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_batch_destroy(edb_batch *b) {
+  if (!b) return EDB_OK;
+  if (b->st) cudaStreamSynchronize(b->st);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  dfree(b->Fhat);
+  dfree(b->F);
+  for (auto &p : b->Fs) dfree(p);
+  for (auto &p : b->Qs) dfree(p);
+  dfree(b->in32);
+  dfree(b->state);
+  dfree(b->mom);
+  dfree(b->H);
+  dfree(b->tr_raw);
+  dfree(b->tr_fixed);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+  return EDB_OK;
+}
+
+static edb_status batch_init_state(edb_batch *b, cudaStream_t st) {
+  // Fhat = fft(F) in FP64, its FP32 copy, entropy bookkeeping reset
+  EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->F, b->Fhat, nullptr, 0, 0, st));
+  EDB_TRY(launch_d2f(b->n, b->Fhat, b->in32, st));
+  std::vector<EfixState> init((size_t)b->d.S, EfixState{1.0, 0, 0, 1.0, 0, 0});
+  EDB_CUDA(cudaMemcpyAsync(b->state, init.data(), sizeof(EfixState) * b->d.S,
+                           cudaMemcpyHostToDevice, st));
+  EDB_CUDA(cudaStreamSynchronize(st));
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_batch_load(edb_batch *b, const double *F0_real) {
+  if (!b || !F0_real) return fail(EDB_EINVAL, "null argument");
+  double *tmp = nullptr;
+  EDB_TRY(dalloc(&tmp, (size_t)b->n));
+  cudaError_t e = cudaMemcpyAsync(tmp, F0_real, sizeof(double) * b->n, cudaMemcpyHostToDevice, b->st);
+  edb_status rc = e == cudaSuccess ? launch_real_to_complex(b->n, tmp, b->F, b->st)
+                                   : cuda_fail(e, "cudaMemcpyAsync");
+  if (rc == EDB_OK) rc = batch_init_state(b, b->st);
+  cudaStreamSynchronize(b->st);
+  dfree(tmp);
+  return rc;
+}
+
+extern "C" edb_status edb_batch_load_device(edb_batch *b, const double *d_F0_real, void *stream) {
+  if (!b || !d_F0_real) return fail(EDB_EINVAL, "null argument");
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->st;
+  EDB_TRY(launch_real_to_complex(b->n, d_F0_real, b->F, st));
+  return batch_init_state(b, st);
+}
+
+// One step for every solve: Q-hat stages on the FP32 copy of each stage
+// input, stage updates in FP64 (each also refreshing the FP32 copy), then the
+// FP64 ifft + entropy + fix rule when enabled.
+static edb_status batch_step_record(edb_batch *b, cudaStream_t st) {
+  const long long n = b->n;
+  const int S = b->d.S, N = b->d.N;
+  const double dt = b->d.dt;
+  const float *B32 = b->q->B32;
+  double2 *Fh = b->Fhat, **F = b->Fs;
+  float2 **Q = b->Qs, *in = b->in32;
+  auto calq = [&](float2 *out) { return launch_calq32_batch(N, S, B32, in, out, st); };
+  switch (b->d.scheme) {
+    case EDB_SCHEME_FE:
+      EDB_TRY(calq(Q[0]));
+      EDB_TRY(launch_stage_f32q(n, STAGE_AXPY, 0, dt, 0, Fh, Fh, 0, 0, Q[0], 0, 0, 0, in, st));
+      break;
+    case EDB_SCHEME_SSP3:
+      EDB_TRY(calq(Q[0]));
+      EDB_TRY(launch_stage_f32q(n, STAGE_AXPY, 0, dt, 0, F[0], Fh, 0, 0, Q[0], 0, 0, 0, in, st));
+      EDB_TRY(calq(Q[0]));
+      EDB_TRY(launch_stage_f32q(n, STAGE_SSP3_2, 0, 0.25 * dt, 0, F[1], Fh, F[0], 0, Q[0], 0, 0, 0,
+                                in, st));
+      EDB_TRY(calq(Q[0]));
+      EDB_TRY(launch_stage_f32q(n, STAGE_SSP3_3, 0, 2. / 3. * dt, 0, Fh, Fh, F[1], 0, Q[0], 0, 0,
+                                0, in, st));
+      break;
+    case EDB_SCHEME_RK4:
+      EDB_TRY(calq(Q[0]));
+      EDB_TRY(
+          launch_stage_f32q(n, STAGE_AXPY, 0, 0.5 * dt, 0, F[0], Fh, 0, 0, Q[0], 0, 0, 0, in, st));
+      EDB_TRY(calq(Q[1]));
+      EDB_TRY(
+          launch_stage_f32q(n, STAGE_AXPY, 0, 0.5 * dt, 0, F[1], Fh, 0, 0, Q[1], 0, 0, 0, in, st));
+      EDB_TRY(calq(Q[2]));
+      EDB_TRY(launch_stage_f32q(n, STAGE_AXPY, 0, dt, 0, F[2], Fh, 0, 0, Q[2], 0, 0, 0, in, st));
+      EDB_TRY(calq(Q[3]));
+      EDB_TRY(launch_stage_f32q(n, STAGE_RK4, 0, dt / 6., 0, Fh, Fh, 0, 0, Q[0], Q[1], Q[2], Q[3],
+                                in, st));
+      break;
+  }
+  if (b->d.fix_entropy) {
+    EDB_TRY(launch_dft3d(N, S, Fh, b->F, nullptr, 1, 0, st));
+    EDB_TRY(launch_step_entropy(N, S, b->d.R, b->F, b->state, 1.0e-10, 2, b->tr_raw, b->tr_fixed,
+                                1, st));
+  }
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_batch_step(edb_batch *b, int nsteps, void *stream) {
+  if (!b) return fail(EDB_EINVAL, "null handle");
+  if (nsteps < 0) return fail(EDB_EINVAL, "nsteps must be >= 0");
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->st;
+  if (!b->exec) {
+    long long before = g_launches.load();
+    cudaGraph_t graph = nullptr;
+    EDB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    edb_status rc = batch_step_record(b, st);
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (rc != EDB_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&b->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    b->launches_per_step = (int)(g_launches.load() - before);
+    g_launches -= b->launches_per_step;  // captured, not executed
+  }
+  for (int i = 0; i < nsteps; ++i) {
+    EDB_CUDA(cudaGraphLaunch(b->exec, st));
+    count_launch(b->launches_per_step);
+  }
+  if (!stream) EDB_CUDA(cudaStreamSynchronize(st));
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat) {
+  if (!b) return fail(EDB_EINVAL, "null handle");
+  cudaStream_t st = b->st;
+  EDB_CUDA(cudaStreamSynchronize(st));
+  if (Fhat)
+    EDB_CUDA(cudaMemcpy(Fhat, b->Fhat, sizeof(double2) * b->n, cudaMemcpyDeviceToHost));
+  if (F_real) {
+    EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->Fhat, b->F, nullptr, 1, 0, st));
+    std::vector<double2> tmp((size_t)b->n);
+    EDB_CUDA(cudaMemcpyAsync(tmp.data(), b->F, sizeof(double2) * b->n, cudaMemcpyDeviceToHost, st));
+    EDB_CUDA(cudaStreamSynchronize(st));
+    for (long long i = 0; i < b->n; ++i) F_real[i] = tmp[(size_t)i].x;
+  }
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_batch_moments(edb_batch *b, double *moments, double *entropy) {
+  if (!b) return fail(EDB_EINVAL, "null handle");
+  cudaStream_t st = b->st;
+  EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->Fhat, b->F, nullptr, 1, 0, st));
+  EDB_TRY(launch_moments(b->d.N, b->d.S, b->d.R, b->F, b->mom, st));
+  EDB_TRY(launch_calentropy(b->d.N, b->d.S, b->d.R, b->F, b->H, st));
+  if (moments)
+    EDB_CUDA(cudaMemcpyAsync(moments, b->mom, sizeof(double) * 5 * b->d.S, cudaMemcpyDeviceToHost,
+                             st));
+  if (entropy)
+    EDB_CUDA(cudaMemcpyAsync(entropy, b->H, sizeof(double) * b->d.S, cudaMemcpyDeviceToHost, st));
+  EDB_CUDA(cudaStreamSynchronize(st));
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_batch_launches_per_step(edb_batch *b, int *n) {
+  if (!b || !n) return fail(EDB_EINVAL, "null argument");
+  *n = b->launches_per_step;
+  return EDB_OK;
+}
+
+// ============================================================ measurement aid
+// FP32 FMA issue-rate probe: every thread runs 8 independent FFMA chains.
+// Used as the measured denominator of the FP32 roofline fraction.
+__global__ void ffma_peak_kernel(int iters, float seed, float *out) {
+  float a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = seed + threadIdx.x * 1e-7f + j;
+  const float m = 0.999999f, c = 1e-7f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = fmaf(a[j], m, c);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += a[j];
+  if (s == 12345.678f) out[blockIdx.x] = s;  // keeps the chains alive
+}
+
+extern "C" edb_status edb_measure_fp32_peak(double *tflops) {
+  if (!tflops) return fail(EDB_EINVAL, "null output");
+  EDB_TRY(ensure_device());
+  int dev = 0, sms = 0;
+  EDB_CUDA(cudaGetDevice(&dev));
+  EDB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  float *out = nullptr;
+  EDB_TRY(dalloc(&out, (size_t)sms * 8));
+  const int iters = 20000, threads = 512, blocks = sms * 4;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  ffma_peak_kernel<<<blocks, threads>>>(iters / 10, 1.0f, out);  // warm-up
+  cudaEventRecord(e0);
+  ffma_peak_kernel<<<blocks, threads>>>(iters, 1.0f, out);
+  cudaEventRecord(e1);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  dfree(out);
+  if (e != cudaSuccess) return cuda_fail(e, "ffma probe");
+  double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return EDB_OK;
+}

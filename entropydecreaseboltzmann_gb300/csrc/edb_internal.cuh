@@ -1,0 +1,126 @@
+// Internal declarations shared by the libedb translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/edb.h"
+
+namespace edb {
+
+// ---------------------------------------------------------------- errors
+void set_error(const std::string &msg);
+edb_status fail(edb_status s, const std::string &msg);
+edb_status cuda_fail(cudaError_t e, const char *what);
+void count_launch(int n = 1);
+
+#define EDB_CUDA(call)                                       \
+  do {                                                       \
+    cudaError_t e__ = (call);                                \
+    if (e__ != cudaSuccess) return ::edb::cuda_fail(e__, #call); \
+  } while (0)
+
+#define EDB_TRY(call)                  \
+  do {                                 \
+    edb_status s__ = (call);           \
+    if (s__ != EDB_OK) return s__;     \
+  } while (0)
+
+// Launch check: records the launch and returns on a launch error.
+#define EDB_LAUNCHED()                                        \
+  do {                                                        \
+    ::edb::count_launch();                                    \
+    cudaError_t e__ = cudaGetLastError();                     \
+    if (e__ != cudaSuccess) return ::edb::cuda_fail(e__, "kernel launch"); \
+  } while (0)
+
+edb_status ensure_device();
+
+// ------------------------------------------------------------ parameters
+// Index parameters of one collision sum (both index modes).  With i the
+// centred l-index per dimension (i in [0,N)) and j the k-index (j in [0,P)):
+//   f_l  = fin[(i + sL) mod N]            (FFTW index, per dimension)
+//   f_m  = fin[(j - i + sM) mod N]
+//   beta = B[lflat * KC + kflat]
+// REFERENCE: P = 2n+1, sL = n+1, sM = 2n+1 (QCalculator.h:239-247 with the
+// doubled f of transf :108-123).  ALIASED: P = N, sL = N-n, sM = 0.
+struct QParams {
+  int N, n, P, mode;
+  int sL, sM;
+  long long NQ, KC;  // N^3, P^3
+};
+QParams make_qparams(int N, int mode);
+
+// ------------------------------------------------------------ kernels API
+// genB: table of F(sqrt(a) lp, sqrt(b) lp) for a, b in [0, amax], a = b mod 4.
+edb_status launch_ftable(int N, double gamma, double *d_T, int amax, cudaStream_t st);
+// sigma (filter) per centred index and Bmm per flat centred index.
+edb_status launch_bmm(int N, double gamma, double L, int filter, int mode, const double *d_T,
+                      int amax, double *d_sigma, double *d_Bmm, cudaStream_t st);
+// B64: [l][k] centred, N^3 x N^3 doubles.  B32 (optional): FFTW order floats.
+edb_status launch_genB(int N, double gamma, double L, int filter, int mode, const double *d_T,
+                       int amax, const double *d_sigma, const double *d_Bmm, double *d_B64,
+                       float *d_B32, cudaStream_t st);
+
+// FP64 calQ: partial sums over l-chunks then an ordered reduction + output
+// conversion.  d_partial holds nchunk * KC complex doubles.
+int calq64_nchunk(const QParams &p);
+edb_status launch_calq64(const QParams &p, const double *d_B, const double2 *d_fin,
+                         double2 *d_partial, double2 *d_Q, cudaStream_t st);
+
+// Batched FP32 calQ (ALIASED): S solves, B32 in FFTW order.
+edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin,
+                               float2 *d_Q, cudaStream_t st);
+
+// Batched cubic DFT (FP64 or FP32), out-of-place; d_tmp holds batch*N^3 complex.
+edb_status launch_dft3d(int N, int batch, const void *d_in, void *d_out, void *d_tmp,
+                        int inverse, int fp32, cudaStream_t st);
+
+// Entropy / EntropyFix state per solve.
+struct EfixState {
+  double avg;       // Averagef (EntropyFix.h:20)
+  int avg_flag;     // Average_flag (EntropyFix.h:22)
+  int pad;
+  double H_prev;    // entropy0 of the integrator loop
+  int step;         // integrator step counter (BKW.h:216, 278, ...)
+  int rec;          // trace records written
+};
+
+// calEntropy (BKW.h:140-152) of Re F for `batch` solves -> d_H.
+edb_status launch_calentropy(int N, int batch, double R, const double2 *d_F, double *d_H,
+                             cudaStream_t st);
+// The integrator's post-step rule (compute H, fix on entropy rise, record
+// trace, roll H_prev) for `batch` solves; fix_mode: 0 never, 1 after step>1
+// if flag (FE), 2 if step (CFE with flag / SSP3 / RK4).
+edb_status launch_step_entropy(int N, int batch, double R, double2 *d_F, EfixState *d_state,
+                               double eps, int fix_mode, double *d_trace_raw,
+                               double *d_trace_fixed, int trace_cap, cudaStream_t st);
+// EntropyFix primitives on one array (host API wrappers).
+edb_status launch_efix_average(int Nf, const double *d_f, EfixState *d_state, cudaStream_t st);
+edb_status launch_efix_entropy(int Nf, const double *d_f, EfixState *d_state, double eps,
+                               double *d_H, cudaStream_t st);
+edb_status launch_efix_fixsol(int Nf, double *d_f, EfixState *d_state, double eps, double aim,
+                              cudaStream_t st);
+
+// Stage updates of the integrators (see edb_kernels_misc.cu for the exact
+// expressions).  launch_stage_f32q reads FP32 Q-hat arrays.
+enum { STAGE_AXPY = 0, STAGE_SSP3_2 = 1, STAGE_SSP3_3 = 2, STAGE_RK4 = 3, STAGE_DUFORT = 4 };
+edb_status launch_stage(long long n, int op, double c0, double c1, double c2, double2 *y,
+                        const double2 *x, const double2 *z, const double2 *w, const double2 *q0,
+                        const double2 *q1, const double2 *q2, const double2 *q3, float2 *y32,
+                        cudaStream_t st);
+edb_status launch_stage_f32q(long long n, int op, double c0, double c1, double c2, double2 *y,
+                             const double2 *x, const double2 *z, const double2 *w,
+                             const float2 *q0, const float2 *q1, const float2 *q2,
+                             const float2 *q3, float2 *y32, cudaStream_t st);
+edb_status launch_d2f(long long n, const double2 *x, float2 *y, cudaStream_t st);
+edb_status launch_f2d(long long n, const float2 *x, double2 *y, cudaStream_t st);
+edb_status launch_real_to_complex(long long n, const double *x, double2 *y, cudaStream_t st);
+edb_status launch_sinusoid_init(int N, double R, double2 *d_F, cudaStream_t st);
+// moments (mass, momentum, energy) of Re F per solve, FP64.
+edb_status launch_moments(int N, int batch, double R, const double2 *d_F, double *d_out,
+                          cudaStream_t st);
+
+}  // namespace edb

@@ -1,0 +1,235 @@
+/*
+ * edb.h — C ABI of libedb.so, the GB300 (sm_103a) spectral collision step.
+ *
+ * The reference (YK2015/EntropyDecreaseBoltzmann) is header-only C++ with no C
+ * ABI; its call surface for this path is the class trio
+ *   QCalculator<c_type,r_type>  (CalQ/QCalculator.h:17-62)
+ *   fft3d                       (CalQ/fft3d.h:17-49)
+ *   EntropyFix<i_type,r_type>   (CalQ/EntropyFix.h:13-46)
+ * driven by BKW3D's integrators (CalQ/BKW.h:191-633).  Each entry point below
+ * names the reference interface it replaces.  The drop-in C++ headers under
+ * entropydecreaseboltzmann_gb300/cpp/ wrap these functions in classes with
+ * the reference's names and signatures.
+ *
+ * Conventions
+ *  - Complex arrays are interleaved (re, im) doubles (or floats for the
+ *    batched FP32 path), N^3 entries, row-major [i][j][k], k fastest, in FFTW
+ *    frequency order — the memory layout of std::complex<double>[N^3] and
+ *    fftw_complex[N^3] used by the reference.
+ *  - Functions taking host pointers are synchronous.  Functions with a
+ *    `_device` suffix take device pointers and a cudaStream_t (passed as
+ *    void*, NULL = default stream) and are stream-ordered.
+ *  - Every function returns an edb_status; edb_last_error() gives text for
+ *    the calling thread's last failure.  The reference has no error codes
+ *    (it asserts, EntropyFix.h:127,214).
+ *  - Handles are not thread-safe (the reference's classes are not either:
+ *    QCalculator::calQ mutates member scratch, QCalculator.h:27-29); use one
+ *    handle per host thread.
+ *  - There is no CPU fallback: without a usable sm_103a GPU every compute
+ *    entry point fails with EDB_ECUDA.
+ */
+#ifndef EDB_H
+#define EDB_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  EDB_OK = 0,
+  EDB_EINVAL = 1,     /* bad argument */
+  EDB_ENOMEM = 2,     /* device or host allocation failed / over budget */
+  EDB_ECUDA = 3,      /* CUDA runtime error, or no usable GPU */
+  EDB_ETIMEDOUT = 4,  /* a bounded device wait ran out */
+  EDB_ENOTREADY = 5,  /* state not initialised (e.g. calQ before genB) */
+  EDB_EBUSY = 6,      /* resource in use (e.g. server slots full) */
+  EDB_ENOTFOUND = 7   /* unknown request id */
+} edb_status;
+
+/* Index modes of the collision sum.
+ * REFERENCE: the reference's literal loops (QCalculator.h:181-183, 239-253).
+ *   For even N these run (2n+1)^3 = (N-1)^3 columns against an N^3 row
+ *   stride, exactly as the reference does.
+ * ALIASED: Q_k = sum_l f_l f_((k-l) mod N) beta(l,k) over modes
+ *   [-n, N-1-n]^3, n = (N-1)/2; identical to REFERENCE for odd N. */
+#define EDB_INDEX_REFERENCE 0
+#define EDB_INDEX_ALIASED 1
+
+/* Box half-width hard-coded in the reference's kernel scale
+ * (QCalculator.h:176: rval = 4 pi (2 lambda/pi * 6.62132/N)^(3+alpha)). */
+#define EDB_R_REFERENCE 6.62132
+
+/* Time integrators of BKW3D (BKW.h:54-59). */
+#define EDB_SCHEME_FE 0     /* BKW3D::FEuler, BKW.h:191-251 */
+#define EDB_SCHEME_CFE 1    /* BKW3D::CFE,    BKW.h:254-313 */
+#define EDB_SCHEME_RK2 2    /* BKW3D::RK2,    BKW.h:314-384 */
+#define EDB_SCHEME_SSP3 3   /* BKW3D::SSP3,   BKW.h:387-449 */
+#define EDB_SCHEME_RK4 4    /* BKW3D::RK4,    BKW.h:452-519 */
+#define EDB_SCHEME_DUFORT 5 /* BKW3D::DUFORT, BKW.h:522-633 */
+
+const char *edb_last_error(void);
+const char *edb_status_string(edb_status s);
+int edb_version(void);
+/* Number of kernels this library has launched since load (all devices). */
+long long edb_kernel_launch_count(void);
+/* Measured FP32 FMA throughput of the current device in TFLOP/s (a short
+ * probe kernel); the denominator of the batched kernel's roofline fraction.
+ * No reference counterpart (the reference has no GPU code). */
+edb_status edb_measure_fp32_peak(double *tflops);
+
+/* ------------------------------------------------------------ QCalculator */
+
+/* Constructor arguments of QCalculator(N, alpha) (QCalculator.h:39), plus the
+ * generalisations the reference hard-codes: the VHS exponent as a real number
+ * (alpha is an int 0/1 there, :31), the box half-width L in rval (:176), the
+ * filter switch (closeFilter, :54) and the index mode. */
+typedef struct {
+  int N;           /* modes per dimension, 3 <= N <= 64 */
+  double gamma;    /* VHS exponent; 0 = Maxwell molecules, 1 = hard spheres */
+  double L;        /* box half-width used in rval; EDB_R_REFERENCE reproduces the reference */
+  int filter;      /* 1 = the reference default (IS_FILTER = 1, :34); 0 = closeFilter() */
+  int index_mode;  /* EDB_INDEX_REFERENCE or EDB_INDEX_ALIASED */
+} edb_qcalc_desc;
+
+typedef struct edb_qcalc edb_qcalc;
+
+/* Fills the reference defaults for QCalculator(N, alpha): gamma = alpha,
+ * L = 6.62132, filter on, REFERENCE index mode. */
+edb_status edb_qcalc_desc_init(edb_qcalc_desc *d, int N, int alpha);
+
+/* QCalculator(N, alpha) (QCalculator.h:39-52).  Allocates nothing on the
+ * device until genB. */
+edb_status edb_qcalc_create(const edb_qcalc_desc *d, edb_qcalc **out);
+/* ~QCalculator (QCalculator.h:38). */
+edb_status edb_qcalc_destroy(edb_qcalc *q);
+/* closeFilter (QCalculator.h:54); call before genB. */
+edb_status edb_qcalc_close_filter(edb_qcalc *q);
+
+/* genB (QCalculator.h:158-229) on the device in FP64: the N^3 x N^3 table
+ * beta(l, k), plus (ALIASED mode) its FP32 copy in FFTW order for the batched
+ * path.  gamma outside {0,1} uses Gauss-Legendre quadrature of
+ * F_gamma = int_0^1 r^(2+gamma) sinc(xi r) sinc(eta r) dr (ReadMe.md:51). */
+edb_status edb_qcalc_genB(edb_qcalc *q);
+
+/* virtual calQ(Qout, fin) (QCalculator.h:59, 231-257): FP64, host buffers,
+ * synchronous.  fin and Qout hold N^3 interleaved complex doubles. */
+edb_status edb_qcalc_calQ(edb_qcalc *q, const double *fin, double *Qout);
+
+/* Same as edb_qcalc_calQ on device buffers, stream-ordered. */
+edb_status edb_qcalc_calQ_device(edb_qcalc *q, const double *d_fin, double *d_Qout,
+                                 void *stream);
+
+/* Batched Q-hat for S independent solves sharing this handle's B table
+ * (ALIASED mode only): d_fin / d_Qout hold S x N^3 interleaved complex
+ * floats (FFTW order), solve-major.  Complex FP32 arithmetic with
+ * compensated (two-sum) accumulation across blocks of the l-sum. */
+edb_status edb_qcalc_calQ_batch_f32_device(edb_qcalc *q, int S, const float *d_fin,
+                                           float *d_Qout, void *stream);
+
+/* Copies count entries of the FP64 B table starting at flat index first
+ * (row-major [l][k], centred indices) to host memory. */
+edb_status edb_qcalc_copy_B(edb_qcalc *q, long long first, long long count, double *host_out);
+/* Sets the FP64 B table from host memory (all N^6 entries); used to run calQ
+ * on a table produced elsewhere. */
+edb_status edb_qcalc_set_B(edb_qcalc *q, const double *host_B);
+
+typedef struct {
+  int N, n, P;          /* P = 2n+1 (REFERENCE) or N (ALIASED): k extent per dimension */
+  long long NQ;         /* N^3 */
+  long long terms;      /* terms of one calQ: N^3 P^3 */
+  long long B_bytes;    /* FP64 table bytes */
+  int has_B32;          /* FP32 FFTW-order copy present */
+} edb_qcalc_info;
+edb_status edb_qcalc_get_info(edb_qcalc *q, edb_qcalc_info *out);
+
+/* ------------------------------------------------------------------ fft3d */
+
+/* fft3d::fft(Nx,Ny,Nz, re, fre) (fft3d.h:25-30): fre = unnormalised forward
+ * DFT (sign -1) of re.  Host buffers, FP64, synchronous. */
+edb_status edb_fft3d_fft(int nx, int ny, int nz, const double *re, double *fre);
+/* fft3d::ifft(Nx,Ny,Nz, re, fre) (fft3d.h:32-48): re = backward DFT of fre
+ * times 1/(Nx Ny Nz).  Cubes only (the reference's normalisation loop uses
+ * Ny for the third extent, :43). */
+edb_status edb_fft3d_ifft(int nx, int ny, int nz, double *re, const double *fre);
+/* Batched cubic transforms on device buffers: `batch` arrays of N^3 complex,
+ * fp32 = 0 (double) or 1 (float); inverse applies the 1/N^3 factor. */
+edb_status edb_fft3d_device(int N, int batch, const void *d_in, void *d_out, int inverse,
+                            int fp32, void *stream);
+
+/* ------------------------------------------------------------- EntropyFix */
+
+typedef struct edb_efix edb_efix;
+/* EntropyFix(Nt, eps) (EntropyFix.h:29-32). */
+edb_status edb_efix_create(int Nt, double eps, edb_efix **out);
+edb_status edb_efix_destroy(edb_efix *e);
+/* setAverage(Nf, f) (EntropyFix.h:65-78): latches mean(f). */
+edb_status edb_efix_set_average(edb_efix *e, int Nf, const double *f);
+/* EntropyCal(Nf, f) (EntropyFix.h:124-161): mean of f log f over f > eps,
+ * minus the latched average (latched from f on first use). */
+edb_status edb_efix_entropy(edb_efix *e, int Nf, const double *f, double *H);
+/* FixSol(Nf, f, aim) (EntropyFix.h:211-253): bisection for
+ * f <- (1-beta) f + beta * average, in place. */
+edb_status edb_efix_fixsol(edb_efix *e, int Nf, double *f, double aim);
+edb_status edb_efix_get_average(edb_efix *e, double *avg, int *latched);
+
+/* -------------------------------------------------------- BKW3D integrator */
+
+typedef struct {
+  int N;             /* grid points per dimension (BKW3D(N0, R), BKW.h:39) */
+  double R;          /* computational domain [-R, R]^3 */
+  int scheme;        /* EDB_SCHEME_* */
+  int fix_entropy;   /* setFixEntropy (BKW.h:46); FE and CFE consult it, SSP3/RK4 fix regardless */
+  double beta;       /* CFE / DUFORT parameter */
+  edb_qcalc_desc kernel; /* the reference uses QCalculator(N0, 0): gamma 0, L 6.62132, filter on */
+} edb_solver_desc;
+
+typedef struct edb_solver edb_solver;
+edb_status edb_solver_create(const edb_solver_desc *d, edb_solver **out);
+edb_status edb_solver_destroy(edb_solver *s);
+/* Initial data in real space (N^3 interleaved complex); NULL selects the
+ * reference's setInitialValue (BKW.h:121-138, the live funExact branch). */
+edb_status edb_solver_set_initial(edb_solver *s, const double *F0);
+/* Runs the reference loop `do { t += dt; ... } while (t < TEnd)` of the
+ * chosen scheme from T0 (BKW.h:218-248 etc.), entirely on the device: calQ
+ * stages, stage updates, ifft, calEntropy and the entropy-fix rule. */
+edb_status edb_solver_run(edb_solver *s, double T0, double TEnd, double dt, int *nsteps);
+/* Final Fhat (reciprocal space) and F (real space, after any fix). */
+edb_status edb_solver_get(edb_solver *s, double *Fhat, double *F);
+/* Entropy after each step before / after the fix (BKW.h:226-235). */
+edb_status edb_solver_trace(edb_solver *s, double *raw, double *fixed, int cap, int *n);
+
+/* ------------------------------------------- batched solves (FP32 Q-hat) */
+
+typedef struct {
+  int S;             /* number of independent solves */
+  int N;             /* modes per dimension (all solves share the kernel table) */
+  double R;          /* velocity box half-width */
+  int scheme;        /* EDB_SCHEME_FE, EDB_SCHEME_SSP3 or EDB_SCHEME_RK4 */
+  double dt;
+  int fix_entropy;   /* apply the EntropyFix rule after each step (FP64) */
+} edb_batch_desc;
+
+typedef struct edb_batch edb_batch;
+/* Stage state is FP64 on the device; each Q-hat evaluation runs the FP32
+ * compensated batched kernel on an FP32 copy of the stage input. */
+edb_status edb_batch_create(edb_qcalc *q, const edb_batch_desc *d, edb_batch **out);
+edb_status edb_batch_destroy(edb_batch *b);
+/* Real-space initial data, S x N^3 doubles (real), host memory. */
+edb_status edb_batch_load(edb_batch *b, const double *F0_real);
+/* Same, device memory (S x N^3 doubles). */
+edb_status edb_batch_load_device(edb_batch *b, const double *d_F0_real, void *stream);
+/* Advances every solve by nsteps steps (one CUDA graph launch per step). */
+edb_status edb_batch_step(edb_batch *b, int nsteps, void *stream);
+/* Real-space f (S x N^3 doubles) and Fhat (S x N^3 complex) to host memory;
+ * either pointer may be NULL. */
+edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat);
+/* Per-solve moments of the current state: S x 5 doubles (mass, momentum x3,
+ * energy) on the velocity grid, and the entropy H (S doubles). */
+edb_status edb_batch_moments(edb_batch *b, double *moments, double *entropy);
+/* Kernel launches per step of the captured graph. */
+edb_status edb_batch_launches_per_step(edb_batch *b, int *n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EDB_H */
