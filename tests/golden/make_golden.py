@@ -81,6 +81,22 @@ def main():
         out[f"efix_{Nt}"] = np.array([e1, e2, e3, ref.L.edbref_efix_average(h)])
         out[f"efix_fixed_{Nt}"] = g
         ref.L.edbref_efix_free(h)
+    # ---- EntropyFix, well-conditioned: aim halfway between H(f) and H(mean f),
+    # so the bisection root has a nonzero slope
+    for Nt in (64, 4096):
+        f = 1.0 + 0.5 * np.sin(np.arange(Nt) * 0.37) ** 2
+        h = ref.L.edbref_efix_new(Nt, 1.0e-10)
+        e_f = ref.L.edbref_efix_entropy(h, Nt, _ptr(f))
+        avg = ref.L.edbref_efix_average(h)
+        fbar = np.full(Nt, avg)
+        e_bar = ref.L.edbref_efix_entropy(h, Nt, _ptr(fbar))
+        aim = 0.5 * (e_f + e_bar)
+        g = f.copy()
+        ref.L.edbref_efix_fixsol(h, Nt, _ptr(g), aim)
+        e_g = ref.L.edbref_efix_entropy(h, Nt, _ptr(g))
+        out[f"efixwc_{Nt}"] = np.array([e_f, e_bar, aim, e_g, avg])
+        out[f"efixwc_fixed_{Nt}"] = g
+        ref.L.edbref_efix_free(h)
     # ---- initial data / entropy
     for N in (5, 6, 8):
         F0 = ref.initial(N, R)

@@ -91,6 +91,18 @@ def test_entropyfix_matches_reference(oracle, golden, Nt):
     assert np.array_equal(g, golden[f"efix_fixed_{Nt}"])
 
 
+@pytest.mark.parametrize("Nt", [64, 4096])
+def test_entropyfix_well_conditioned_matches_reference(oracle, golden, Nt):
+    f = 1.0 + 0.5 * np.sin(np.arange(Nt) * 0.37) ** 2
+    ref = golden[f"efixwc_{Nt}"]
+    ef = EntropyFixOracle(oracle, Nt)
+    assert ef.EntropyCal(f) == ref[0]
+    g = f.copy()
+    ef.FixSol(g, ref[2])
+    assert np.array_equal(g, golden[f"efixwc_fixed_{Nt}"])
+    assert ef.EntropyCal(g) == ref[3]
+
+
 @pytest.mark.parametrize("N", [5, 6, 8])
 def test_initial_data_and_entropy(oracle, golden, N):
     F0 = oracle.initial_sinusoid(N, R_REFERENCE)
