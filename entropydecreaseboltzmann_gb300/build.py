@@ -28,6 +28,7 @@ UNITS = {
     "edb_kernels_fft.cu": [],
     "edb_kernels_genb.cu": ["-fmad=false"],
     "edb_kernels_misc.cu": ["-fmad=false"],
+    "edb_noalloc.cu": [],
 }
 
 

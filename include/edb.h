@@ -126,6 +126,20 @@ edb_status edb_qcalc_calQ_device(edb_qcalc *q, const double *d_fin, double *d_Qo
 edb_status edb_qcalc_calQ_batch_f32_device(edb_qcalc *q, int S, const float *d_fin,
                                            float *d_Qout, void *stream);
 
+/* FP64 collision sum that allocates nothing, for callers that may not call
+ * cudaMalloc (a host that owns a fixed device pool and accounts for every
+ * byte, a plugin inside such a host, a real-time loop that cannot take
+ * cudaMalloc's implicit synchronisation).  No counterpart in the reference.
+ * The caller passes the FP64 table d_B (N^3 x N^3 doubles, the layout genB
+ * produces; see edb_qcalc_copy_B), d_fin and d_Qout (N^3 complex doubles each,
+ * FFTW order); the result equals edb_qcalc_calQ_device's.  The partial sums
+ * live in one fixed 5 MiB device array per device, which every GPU that loads
+ * the library holds until exit; N must be in [3, 64].  The first call on a
+ * device looks up that array's address, so make it before any stream capture.
+ * Calls that overlap on the GPU share the array and race: serialise them. */
+edb_status edb_calQ_fp64_noalloc(int N, int index_mode, const double *d_B, const double *d_fin,
+                                 double *d_Qout, void *stream);
+
 /* Copies count entries of the FP64 B table starting at flat index first
  * (row-major [l][k], centred indices) to host memory. */
 edb_status edb_qcalc_copy_B(edb_qcalc *q, long long first, long long count, double *host_out);
