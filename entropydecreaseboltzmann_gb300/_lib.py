@@ -68,6 +68,7 @@ def _load():
         "edb_version": (C.c_int, []),
         "edb_kernel_launch_count": (C.c_longlong, []),
         "edb_measure_fp32_peak": (C.c_int, [_dp]),
+        "edb_measure_fp32x2_peak": (C.c_int, [_dp]),
         "edb_qcalc_desc_init": (C.c_int, [C.POINTER(QCalcDesc), C.c_int, C.c_int]),
         "edb_qcalc_create": (C.c_int, [C.POINTER(QCalcDesc), C.POINTER(_vp)]),
         "edb_qcalc_destroy": (C.c_int, [_vp]),
@@ -76,6 +77,8 @@ def _load():
         "edb_qcalc_calQ": (C.c_int, [_vp, _dp, _dp]),
         "edb_qcalc_calQ_device": (C.c_int, [_vp, _vp, _vp, _vp]),
         "edb_qcalc_calQ_batch_f32_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
+        "edb_qcalc_autotune_batch": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _ip]),
+        "edb_device_status": (C.c_int, [_ip, C.c_int]),
         "edb_qcalc_copy_B": (C.c_int, [_vp, C.c_longlong, C.c_longlong, _dp]),
         "edb_qcalc_set_B": (C.c_int, [_vp, _dp]),
         "edb_qcalc_get_info": (C.c_int, [_vp, C.POINTER(QCalcInfo)]),

@@ -17,6 +17,13 @@ from ._lib import (INDEX_REFERENCE, R_REFERENCE, SCHEME_CFE, SCHEME_DUFORT, SCHE
                    SolverDesc, check, devptr, dptr, lib, stream_ptr)
 
 
+def device_status(clear: bool = True) -> int:
+    """Nonzero when a bounded wait inside the batched kernel ran out."""
+    v = C.c_int()
+    check(lib.edb_device_status(C.byref(v), int(clear)))
+    return v.value
+
+
 def kernel_launch_count() -> int:
     """Kernels libedb.so has launched in this process (graph replays included)."""
     return int(lib.edb_kernel_launch_count())
@@ -82,6 +89,13 @@ class QCalculator:
     def calQ_batch_f32(self, S, d_fin, d_Q, stream=None):
         check(lib.edb_qcalc_calQ_batch_f32_device(self._h, int(S), devptr(d_fin), devptr(d_Q),
                                                   stream_ptr(stream)))
+
+    def autotune_batch(self, S, d_fin, d_Q, stream=None):
+        """Pick the fastest batched-kernel variant for S solves; returns its index."""
+        v = C.c_int()
+        check(lib.edb_qcalc_autotune_batch(self._h, int(S), devptr(d_fin), devptr(d_Q),
+                                           stream_ptr(stream), C.byref(v)))
+        return v.value
 
     def B(self, first=0, count=None):
         total = self.NQ * self.NQ

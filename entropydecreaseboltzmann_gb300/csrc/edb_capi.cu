@@ -92,7 +92,22 @@ struct edb_qcalc {
   double2 *fin = nullptr, *Q = nullptr;  // host-API staging
   int nchunk = 0;
   bool ready = false;
+  int c32_variant[16];  // autotuned batched-kernel variant per S bucket, -1 = untuned
 };
+
+// S bucket of the autotuner: floor(log2(number of 16-solve groups)).
+static int s_bucket(int S) {
+  int groups = (S + 15) / 16, b = 0;
+  while (groups > 1 && b < 15) {
+    groups >>= 1;
+    ++b;
+  }
+  return b;
+}
+static int c32_variant_for(const edb_qcalc *q, int S) {
+  int v = q->c32_variant[s_bucket(S)];
+  return v < 0 ? 0 : v;
+}
 
 static edb_status check_desc(const edb_qcalc_desc *d) {
   if (!d) return fail(EDB_EINVAL, "null descriptor");
@@ -120,6 +135,7 @@ extern "C" edb_status edb_qcalc_create(const edb_qcalc_desc *d, edb_qcalc **out)
   EDB_TRY(check_desc(d));
   EDB_TRY(ensure_device());
   edb_qcalc *q = new edb_qcalc();
+  for (int &v : q->c32_variant) v = -1;
   q->d = *d;
   q->p = make_qparams(d->N, d->index_mode);
   cudaError_t e = cudaStreamCreateWithFlags(&q->st, cudaStreamNonBlocking);
@@ -258,7 +274,54 @@ extern "C" edb_status edb_qcalc_calQ_batch_f32_device(edb_qcalc *q, int S, const
     return fail(EDB_EINVAL, "the batched path runs the ALIASED index mode");
   if (!q->ready || !q->B32) return fail(EDB_ENOTREADY, "batched calQ before genB");
   return launch_calq32_batch(q->d.N, S, q->B32, (const float2 *)d_fin, (float2 *)d_Qout,
-                             (cudaStream_t)stream);
+                             (cudaStream_t)stream, c32_variant_for(q, S));
+}
+
+// Times every variant of the batched kernel on the caller's buffers (two
+// launches each after one warm-up, CUDA events on `stream`) and keeps the
+// fastest for this S bucket.
+extern "C" edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float *d_fin,
+                                               float *d_Qout, void *stream, int *chosen) {
+  if (!q || !d_fin || !d_Qout) return fail(EDB_EINVAL, "null argument");
+  if (S < 1) return fail(EDB_EINVAL, "S must be positive");
+  if (!q->ready || !q->B32) return fail(EDB_ENOTREADY, "autotune before genB (ALIASED)");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t e0, e1;
+  EDB_CUDA(cudaEventCreate(&e0));
+  EDB_CUDA(cudaEventCreate(&e1));
+  int best = 0;
+  float best_ms = 1e30f;
+  edb_status rc = EDB_OK;
+  for (int v = 0; v < calq32_variants() && rc == EDB_OK; ++v) {
+    rc = launch_calq32_batch(q->d.N, S, q->B32, (const float2 *)d_fin, (float2 *)d_Qout, st, v);
+    if (rc != EDB_OK) break;
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < 2 && rc == EDB_OK; ++r)
+      rc = launch_calq32_batch(q->d.N, S, q->B32, (const float2 *)d_fin, (float2 *)d_Qout, st, v);
+    cudaEventRecord(e1, st);
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(e, "autotune");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != EDB_OK) return rc;
+  q->c32_variant[s_bucket(S)] = best;
+  if (chosen) *chosen = best;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_device_status(int *status, int clear) {
+  if (!status) return fail(EDB_EINVAL, "null output");
+  return read_calq32_status(status, clear != 0);
 }
 
 // ===================================================================== fft3d
@@ -718,6 +781,11 @@ static edb_status batch_init_state(edb_batch *b, cudaStream_t st) {
   // Fhat = fft(F) in FP64, its FP32 copy, entropy bookkeeping reset
   EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->F, b->Fhat, nullptr, 0, 0, st));
   EDB_TRY(launch_d2f(b->n, b->Fhat, b->in32, st));
+  // pick the batched kernel's variant for this S on real data, before the
+  // step graph is captured (the graph bakes the choice in)
+  if (b->q->c32_variant[s_bucket(b->d.S)] < 0 && !b->exec)
+    EDB_TRY(edb_qcalc_autotune_batch(b->q, b->d.S, (const float *)b->in32, (float *)b->Qs[0], st,
+                                     nullptr));
   std::vector<EfixState> init((size_t)b->d.S, EfixState{1.0, 0, 0, 1.0, 0, 0});
   EDB_CUDA(cudaMemcpyAsync(b->state, init.data(), sizeof(EfixState) * b->d.S,
                            cudaMemcpyHostToDevice, st));
@@ -755,7 +823,8 @@ static edb_status batch_step_record(edb_batch *b, cudaStream_t st) {
   const float *B32 = b->q->B32;
   double2 *Fh = b->Fhat, **F = b->Fs;
   float2 **Q = b->Qs, *in = b->in32;
-  auto calq = [&](float2 *out) { return launch_calq32_batch(N, S, B32, in, out, st); };
+  const int variant = c32_variant_for(b->q, S);
+  auto calq = [&](float2 *out) { return launch_calq32_batch(N, S, B32, in, out, st, variant); };
   switch (b->d.scheme) {
     case EDB_SCHEME_FE:
       EDB_TRY(calq(Q[0]));
@@ -901,6 +970,62 @@ extern "C" edb_status edb_measure_fp32_peak(double *tflops) {
   dfree(out);
   if (e != cudaSuccess) return cuda_fail(e, "ffma probe");
   double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return EDB_OK;
+}
+
+// Packed FP32 (fma.rn.f32x2) issue-rate probe: 8 independent packed chains per
+// thread, 2 FP32 FMAs per instruction.  Compared with edb_measure_fp32_peak it
+// shows whether packed issue raises the FP32 datapath ceiling or only frees
+// issue slots.
+__global__ void ffma2_peak_kernel(int iters, float seed, float *out) {
+  unsigned long long a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    float x = seed + threadIdx.x * 1e-7f + j;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(a[j]) : "f"(x));
+  }
+  unsigned long long m, c;
+  asm("mov.b64 %0, {%1, %1};" : "=l"(m) : "f"(0.999999f));
+  asm("mov.b64 %0, {%1, %1};" : "=l"(c) : "f"(1e-7f));
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) asm("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(a[j]) : "l"(m), "l"(c));
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a[j]));
+    s += lo + hi;
+  }
+  if (s == 12345.678f) out[blockIdx.x] = s;
+}
+
+extern "C" edb_status edb_measure_fp32x2_peak(double *tflops) {
+  if (!tflops) return fail(EDB_EINVAL, "null output");
+  EDB_TRY(ensure_device());
+  int dev = 0, sms = 0;
+  EDB_CUDA(cudaGetDevice(&dev));
+  EDB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  float *out = nullptr;
+  EDB_TRY(dalloc(&out, (size_t)sms * 8));
+  const int iters = 20000, threads = 512, blocks = sms * 4;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  ffma2_peak_kernel<<<blocks, threads>>>(iters / 10, 1.0f, out);
+  cudaEventRecord(e0);
+  ffma2_peak_kernel<<<blocks, threads>>>(iters, 1.0f, out);
+  cudaEventRecord(e1);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  dfree(out);
+  if (e != cudaSuccess) return cuda_fail(e, "ffma2 probe");
+  double flops = 2.0 * 2.0 * 8.0 * iters * (double)threads * blocks;
   *tflops = flops / (ms * 1e-3) / 1e12;
   return EDB_OK;
 }

@@ -71,8 +71,13 @@ edb_status launch_calq64(const QParams &p, const double *d_B, const double2 *d_f
                          double2 *d_partial, double2 *d_Q, cudaStream_t st);
 
 // Batched FP32 calQ (ALIASED): S solves, B32 in FFTW order.
+// variant in [0, calq32_variants()) selects the CTA-size bound (see the kernel).
+int calq32_variants();
 edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin,
-                               float2 *d_Q, cudaStream_t st);
+                               float2 *d_Q, cudaStream_t st, int variant);
+// Reads (and optionally clears) the batched kernel's status word: nonzero
+// when a bounded wait inside it ran out.
+edb_status read_calq32_status(int *status, bool clear);
 
 // Batched cubic DFT (FP64 or FP32), out-of-place; d_tmp holds batch*N^3 complex.
 edb_status launch_dft3d(int N, int batch, const void *d_in, void *d_out, void *d_tmp,

@@ -7,9 +7,8 @@
 // second kernel adds the chunks in a fixed order (deterministic) and applies
 // the output permutation of convertQ (:144-155).
 //
-// Batched FP32 path (many solves sharing one B table, ALIASED mode): a CTA
-// owns a group of solves and a k-tile (one k1, a run of k2, all k3) and walks
-// every l; see calq32_kernel below.
+// Batched FP32 path (many solves sharing one B table, ALIASED mode): see the
+// comment above calq32_kernel.
 #include "edb_internal.cuh"
 
 namespace edb {
@@ -140,31 +139,186 @@ edb_status launch_calq64(const QParams &p, const double *d_B, const double2 *d_f
 }
 
 // ---------------------------------------------------------------------------
-// Batched FP32 kernel.
+// Batched FP32 kernel (ALIASED mode, many solves sharing one table).
 //
-// Work: Q^s_K = sum_L B[L][K] f^s_L f^s_(K-L mod N) for S solves, all indices
+// Work: Q^s_K = sum_L B[L][K] f^s_L f^s_((K-L) mod N) for S solves; every index
 // in FFTW order, B32 row-major [L][K].
 //
-// CTA = (group of SG = SC*WS solves) x (k1, a tile of K2T k2 values, all k3).
-// Thread = (k2, run of A consecutive k3, SC solves).  The WS threads that
-// share a (k2, k3-run) are adjacent lanes, so their B loads coalesce into one
-// transaction.  For each L the thread needs
-//   B[L][k1,k2,k3..k3+A)   A floats, shared by its SC solves,
-//   f^s_L                  one complex per solve (same for the whole CTA),
-//   f^s_(K-L)              A complex per solve; along l3 these form a sliding
-//                          window over m3 = k3 + a - l3, so one new value per
-//                          l3 step is loaded into a ring of A registers.
-// The m1-plane f^s[m1][:][:] (m1 = k1 - l1) of the CTA's solves is staged in
-// shared memory while l1 is fixed.  Sums: plain FP32 FMA along one l3 line
-// (N terms), then a two-sum fold into (hi, lo) per accumulator — blocked
-// compensated summation (fast inner sum, error-free outer sum).
+// CTA = (group of SG = 16 solves) x (one k1, a tile of K2T k2 values, all k3).
+// Thread = (solve pair {w, w+8}, k2, run of A = 8 consecutive k3).  The CTA
+// walks the l-lines (l1, l2) in order; for each line it needs
+//   B[(l1,l2,l3)][k1, k2-tile, all k3]  N rows of K2T*N floats (the B tile),
+//   f^s[l1][l2][:]                       N complex per solve (the f_l line),
+//   f^s[m1][:][:], m1 = k1 - l1          the m1-plane, kept while l1 is fixed.
+// Tile and line are double-buffered in shared memory.  Warp 0 issues the 1-D
+// TMA bulk copies (cp.async.bulk ... mbarrier::complete_tx) of line i+1, one
+// copy per lane, while every warp computes line i; a "full" mbarrier per
+// stage says the data landed, an "empty" mbarrier per stage (one arrival per
+// warp) says every warp is done with it, so warps never wait for each other
+// inside an l1-plane.  All waits are bounded: a wait that runs out marks the
+// thread, the block leaves together at the next block barrier
+// (__syncthreads_or), drains its copies and sets a device status word.
+// Widths that are not multiples of 16 bytes or below 8 (N % 4 != 0, N < 8)
+// take the same compute path with cooperative plain loads instead of TMA.
+//
+// Arithmetic, per term and solve, in three packed f32x2 instructions that carry
+// the six FP32 operations of the term:
+//   q    = (b, b) * f_m                 mul.rn.f32x2
+//   accA = (f_l.x, f_l.x) * q + accA    fma.rn.f32x2
+//   accB = (f_l.y, f_l.y) * q + accB    fma.rn.f32x2
+// so that sum b f_l f_m = (accA.x - accB.y, accA.y + accB.x).  Along l3 the
+// needed f_m = f[m1][m2][k3+a-l3] slide down by one, so they live in a ring of A
+// registers.  Sums are plain FP32 FMA across FOLD_LINES l-lines (FOLD_LINES * N
+// terms per output), then combined and folded into a (hi, lo) two-sum pair:
+// blocked compensated summation.
 // ---------------------------------------------------------------------------
 namespace {
-constexpr int A = 8;   // k3 outputs per thread
-constexpr int SC = 2;  // solves per thread
-constexpr int WS = 8;  // solve subgroups per CTA
-constexpr int SG = SC * WS;
-constexpr int MAX_THREADS = 384;
+constexpr int A = 8;                      // k3 outputs per thread
+constexpr int SC = 2;                     // solves per thread: w and w + WS
+constexpr int WS = 8;                     // solve lanes per (k2, k3-run)
+constexpr int SG = SC * WS;               // solves per CTA
+constexpr int ROWPAD = 8;                 // floats after each B-tile row
+constexpr int FLPAD = 2;                  // complex after each f_l line
+constexpr int PLPAD = 2;                  // complex after each solve's plane
+constexpr int FOLD_LINES = 4;             // l-lines per compensated fold
+constexpr unsigned long long WAIT_LIMIT_NS = 200000000ull;  // 200 ms per mbarrier wait
+
+__device__ int g_calq32_status;  // nonzero: a bounded wait ran out
+
+constexpr int MAX_ST = 4;                 // pipeline stages (l-lines in flight)
+
+struct C32Geom {
+  int N, R, RA, K2T, BROW, FLS, PSTR, NST, NPL;
+  size_t off_B, off_fl, off_pl, bytes;
+};
+
+// Shared-memory layout for a CTA: NST stages of (B tile, f_l lines), NPL
+// m1-planes.  Barriers: full[MAX_ST], empty[MAX_ST], plane[2].
+__host__ __device__ inline C32Geom c32_geom(int N, int K2T, int NST, int NPL) {
+  C32Geom g;
+  g.N = N;
+  g.R = (N + A - 1) / A;
+  g.RA = g.R * A;
+  g.K2T = K2T;
+  g.NST = NST;
+  g.NPL = NPL;
+  g.BROW = K2T * N + ROWPAD;
+  g.FLS = g.RA + FLPAD;
+  g.PSTR = N * N + PLPAD;
+  size_t o = 128;  // 2*MAX_ST + 2 mbarriers (+ pad)
+  g.off_B = o;
+  o += sizeof(float) * (size_t)NST * g.RA * g.BROW;
+  g.off_fl = o;
+  o += sizeof(float2) * (size_t)NST * SG * g.FLS;
+  g.off_pl = o;
+  o += sizeof(float2) * (size_t)NPL * SG * g.PSTR;
+  g.bytes = o;
+  return g;
+}
+
+__device__ __forceinline__ uint32_t s_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(s_addr(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(s_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(s_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(s_addr(dst)),
+      "l"(src), "r"(bytes), "r"(s_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(s_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long gtimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait for the phase with this parity, for at most WAIT_LIMIT_NS.  A thread
+// that already timed out does not wait again (its data are discarded at the
+// next block barrier).
+__device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, bool &to) {
+  if (to) return;
+  if (mbar_try_wait(bar, parity)) return;
+  const unsigned long long t0 = gtimer_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (gtimer_ns() - t0 > WAIT_LIMIT_NS) {
+      to = true;
+      return;
+    }
+  }
+}
+
+typedef unsigned long long u64;
+__device__ __forceinline__ u64 pk(float a, float b) {
+  u64 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ u64 ld_pk(const float2 *p) {
+  return *reinterpret_cast<const u64 *>(p);
+}
+__device__ __forceinline__ float2 upk(u64 v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+__device__ __forceinline__ u64 mul2(u64 a, u64 b) {
+  u64 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ void fma2(u64 &acc, u64 a, u64 b) {
+  asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc) : "l"(a), "l"(b));
+}
+__device__ __forceinline__ u64 fma2r(u64 a, u64 b, u64 c) {
+  u64 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ u64 add2(u64 a, u64 b) {
+  u64 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ u64 sub2(u64 a, u64 b) {
+  u64 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+// (x.y, x.x)
+__device__ __forceinline__ u64 swp(u64 v) {
+  float2 f = upk(v);
+  return pk(f.y, f.x);
+}
+// Two-sum fold of a packed pair of partial sums into packed (hi, lo).
+__device__ __forceinline__ void two_sum_fold2(u64 &hi, u64 &lo, u64 x) {
+  const u64 s = add2(hi, x);
+  const u64 bb = sub2(s, hi);
+  const u64 e = add2(sub2(hi, sub2(s, bb)), sub2(x, bb));
+  hi = s;
+  lo = add2(lo, e);
+}
 
 __device__ __forceinline__ void two_sum_fold(float &hi, float &lo, float x) {
   float s = hi + x;
@@ -173,162 +327,401 @@ __device__ __forceinline__ void two_sum_fold(float &hi, float &lo, float x) {
   hi = s;
   lo += e;
 }
-}  // namespace
 
-__global__ void __launch_bounds__(MAX_THREADS, 1)
-    calq32_kernel(int N, int S, int K2T, const float *__restrict__ B32,
-                  const float2 *__restrict__ fin, float2 *__restrict__ Q) {
-  extern __shared__ float4 smem_f4[];
-  float2 *fplane = reinterpret_cast<float2 *>(smem_f4);  // [m2][m3][SG]
-  const long long NQ = (long long)N * N * N;
-  const int NN = N * N;
-  const int R = (N + A - 1) / A;
-  const int tid = threadIdx.x;
-  const int w = tid % WS;
-  const int rest = tid / WS;
-  const int r = rest % R;
-  const int k2l = rest / R;
-  const int k1 = blockIdx.y;
-  const int k2 = blockIdx.z * K2T + k2l;
-  const bool k_ok = (k2l < K2T) && (k2 < N);
-  const int k2c = k2 < N ? k2 : N - 1;
-  const int k3_0 = r * A;
-  const int s0 = blockIdx.x * SG;
-  const int sA = s0 + w * SC;  // first solve of this thread
-
-  float2 hi[A][SC], lo[A][SC];
-#pragma unroll
-  for (int a = 0; a < A; ++a)
-#pragma unroll
-    for (int c = 0; c < SC; ++c) {
-      hi[a][c] = make_float2(0.f, 0.f);
-      lo[a][c] = make_float2(0.f, 0.f);
+// Issue (TMA: warp 0, one copy per lane) or perform (plain: all threads) the
+// staging of the B tile and f_l line of line li into buffer `st`.
+template <bool TMA>
+__device__ __forceinline__ void stage_line(const C32Geom &g, int li, int st, int k1, int k2_0,
+                                           int k2n, int s0, int nval, long long NQ,
+                                           const float *__restrict__ B32,
+                                           const float2 *__restrict__ fin, float *Bs,
+                                           float2 *fls, uint64_t *full) {
+  const int N = g.N;
+  float *Bd = Bs + (size_t)st * g.RA * g.BROW;
+  float2 *fd = fls + (size_t)st * SG * g.FLS;
+  const float *Bsrc = B32 + (long long)li * N * NQ + (long long)k1 * N * N + (long long)k2_0 * N;
+  const float2 *fsrc = fin + (long long)s0 * NQ + (long long)li * N;
+  const int rowlen = k2n * N;
+  if (TMA) {  // called by warp 0 only
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) mbar_expect_tx(full + st, (uint32_t)(N * rowlen * 4 + nval * N * 8));
+    __syncwarp();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    for (int l3 = lane; l3 < N; l3 += 32)
+      bulk_g2s(Bd + (size_t)l3 * g.BROW, Bsrc + (long long)l3 * NQ, rowlen * 4, full + st);
+    for (int s = lane; s < nval; s += 32)
+      bulk_g2s(fd + (size_t)s * g.FLS, fsrc + (long long)s * NQ, N * 8, full + st);
+  } else {
+    for (int e = threadIdx.x; e < N * rowlen; e += blockDim.x) {
+      int l3 = e / rowlen, c = e % rowlen;
+      Bd[(size_t)l3 * g.BROW + c] = __ldg(Bsrc + (long long)l3 * NQ + c);
     }
-
-  const bool vec = (N % 4) == 0;
-  const int NL3 = R * A;
-
-  for (int l1 = 0; l1 < N; ++l1) {
-    const int m1 = (k1 - l1 + N) % N;
-    __syncthreads();
-    for (int idx = tid; idx < NN * SG; idx += blockDim.x) {
-      int sl = idx / NN, pos = idx % NN;
-      int s = s0 + sl;
-      float2 v = make_float2(0.f, 0.f);
-      if (s < S) v = __ldg(&fin[(long long)s * NQ + (long long)m1 * NN + pos]);
-      fplane[(long long)pos * SG + sl] = v;
-    }
-    __syncthreads();
-    for (int l2 = 0; l2 < N; ++l2) {
-      const int m2 = (k2c - l2 + N) % N;
-      const float2 *fp = fplane + (long long)m2 * N * SG + w * SC;
-      const float *Brow = B32 + (long long)((l1 * N + l2) * N) * NQ + (long long)k1 * NN +
-                          (long long)k2c * N + k3_0;
-      const float2 *fL[SC];
-#pragma unroll
-      for (int c = 0; c < SC; ++c) {
-        int s = sA + c < S ? sA + c : S - 1;
-        fL[c] = fin + (long long)s * NQ + (long long)(l1 * N + l2) * N;
-      }
-      float2 acc[A][SC];
-#pragma unroll
-      for (int a = 0; a < A; ++a)
-#pragma unroll
-        for (int c = 0; c < SC; ++c) acc[a][c] = make_float2(0.f, 0.f);
-      float2 ring[A][SC];
-#pragma unroll
-      for (int a = 0; a < A; ++a) {
-        int idx = (k3_0 + a) % N;
-#pragma unroll
-        for (int c = 0; c < SC; ++c) ring[a][c] = fp[idx * SG + c];
-      }
-      for (int g = 0; g < NL3; g += A) {
-        int base = (k3_0 - g) % N;
-        if (base < 0) base += N;
-#pragma unroll
-        for (int t = 0; t < A; ++t) {
-          const int l3 = g + t;
-          if (l3 > 0) {
-            int idx = base - t;
-            while (idx < 0) idx += N;
-            const int slot = (A - t) % A;
-#pragma unroll
-            for (int c = 0; c < SC; ++c) ring[slot][c] = fp[idx * SG + c];
-          }
-          const bool valid = l3 < N;
-          float bv[A];
-          const float *bp = Brow + (long long)(valid ? l3 : 0) * NQ;
-          if (vec) {
-            float4 b0 = __ldg(reinterpret_cast<const float4 *>(bp));
-            float4 b1 = __ldg(reinterpret_cast<const float4 *>(bp) + 1);
-            bv[0] = b0.x; bv[1] = b0.y; bv[2] = b0.z; bv[3] = b0.w;
-            bv[4] = b1.x; bv[5] = b1.y; bv[6] = b1.z; bv[7] = b1.w;
-          } else {
-#pragma unroll
-            for (int a = 0; a < A; ++a) bv[a] = __ldg(bp + a);
-          }
-          float2 fl[SC];
-#pragma unroll
-          for (int c = 0; c < SC; ++c)
-            fl[c] = valid ? __ldg(fL[c] + l3) : make_float2(0.f, 0.f);
-#pragma unroll
-          for (int a = 0; a < A; ++a) {
-            const int slot = (a - t + A) % A;
-#pragma unroll
-            for (int c = 0; c < SC; ++c) {
-              const float2 fm = ring[slot][c];
-              const float pr = fl[c].x * fm.x - fl[c].y * fm.y;
-              const float pi = fl[c].x * fm.y + fl[c].y * fm.x;
-              acc[a][c].x = fmaf(bv[a], pr, acc[a][c].x);
-              acc[a][c].y = fmaf(bv[a], pi, acc[a][c].y);
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int a = 0; a < A; ++a)
-#pragma unroll
-        for (int c = 0; c < SC; ++c) {
-          two_sum_fold(hi[a][c].x, lo[a][c].x, acc[a][c].x);
-          two_sum_fold(hi[a][c].y, lo[a][c].y, acc[a][c].y);
-        }
-    }
-  }
-  if (!k_ok) return;
-#pragma unroll
-  for (int c = 0; c < SC; ++c) {
-    const int s = sA + c;
-    if (s >= S) continue;
-    float2 *qp = Q + (long long)s * NQ + (long long)k1 * NN + (long long)k2 * N;
-#pragma unroll
-    for (int a = 0; a < A; ++a) {
-      const int k3 = k3_0 + a;
-      if (k3 < N) qp[k3] = make_float2(hi[a][c].x + lo[a][c].x, hi[a][c].y + lo[a][c].y);
+    for (int e = threadIdx.x; e < nval * N; e += blockDim.x) {
+      int s = e / N, l3 = e % N;
+      fd[(size_t)s * g.FLS + l3] = __ldg(fsrc + (long long)s * NQ + l3);
     }
   }
 }
 
+template <bool TMA>
+__device__ __forceinline__ void stage_plane(const C32Geom &g, int m1, int s0, int nval,
+                                            long long NQ, const float2 *__restrict__ fin,
+                                            float2 *pl, uint64_t *bar) {
+  const int NN = g.N * g.N;
+  const float2 *src = fin + (long long)s0 * NQ + (long long)m1 * NN;
+  if (TMA) {  // warp 0 only
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) mbar_expect_tx(bar, (uint32_t)(nval * NN * 8));
+    __syncwarp();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    for (int s = lane; s < nval; s += 32)
+      bulk_g2s(pl + (size_t)s * g.PSTR, src + (long long)s * NQ, NN * 8, bar);
+  } else {
+    for (int e = threadIdx.x; e < nval * NN; e += blockDim.x) {
+      int s = e / NN, p = e % NN;
+      pl[(size_t)s * g.PSTR + p] = __ldg(src + (long long)s * NQ + p);
+    }
+  }
+}
+
+// One l-line for this thread: A outputs x SC solves.  BIGN: N >= A, so one
+// conditional add brings a ring index back into [0, N).  VEC: N % 4 == 0, so
+// every B-tile row offset is 16-byte aligned and B is read with float4 loads;
+// otherwise with scalar loads.
+template <bool BIGN, bool VEC>
+__device__ __forceinline__ void compute_line(const C32Geom &g, const float *Bt, const float2 *fl0,
+                                             const float2 *fl1, const float2 *p0,
+                                             const float2 *p1, int k3_0, u64 (&accA)[A][SC],
+                                             u64 (&accB)[A][SC]) {
+  const int N = g.N;
+  u64 ring[A][SC];
+#pragma unroll
+  for (int a = 0; a < A; ++a) {
+    int idx = k3_0 + a;
+    if (BIGN) {
+      idx -= (idx >= N) ? N : 0;
+    } else {
+      while (idx >= N) idx -= N;
+    }
+    ring[a][0] = ld_pk(p0 + idx);
+    ring[a][1] = ld_pk(p1 + idx);
+  }
+  for (int gg = 0; gg < g.R; ++gg) {
+    int base = k3_0 - gg * A;
+    if (BIGN) {
+      base += (base < 0) ? N : 0;
+    } else {
+      while (base < 0) base += N;
+    }
+#pragma unroll
+    for (int t = 0; t < A; ++t) {
+      const int l3 = gg * A + t;
+      if (t > 0 || gg > 0) {
+        int idx = base - t;
+        if (BIGN) {
+          idx += (idx < 0) ? N : 0;
+        } else {
+          while (idx < 0) idx += N;
+        }
+        const int slot = (A - t) % A;
+        ring[slot][0] = ld_pk(p0 + idx);
+        ring[slot][1] = ld_pk(p1 + idx);
+      }
+      float bv[A];
+      if (VEC) {
+        const float4 b0 = *reinterpret_cast<const float4 *>(Bt + (size_t)l3 * g.BROW);
+        const float4 b1 = *reinterpret_cast<const float4 *>(Bt + (size_t)l3 * g.BROW + 4);
+        bv[0] = b0.x; bv[1] = b0.y; bv[2] = b0.z; bv[3] = b0.w;
+        bv[4] = b1.x; bv[5] = b1.y; bv[6] = b1.z; bv[7] = b1.w;
+      } else {
+#pragma unroll
+        for (int a = 0; a < A; ++a) bv[a] = Bt[(size_t)l3 * g.BROW + a];
+      }
+      const float2 f0 = fl0[l3], f1 = fl1[l3];
+      const u64 flx[SC] = {pk(f0.x, f0.x), pk(f1.x, f1.x)};
+      const u64 fly[SC] = {pk(f0.y, f0.y), pk(f1.y, f1.y)};
+#pragma unroll
+      for (int a = 0; a < A; ++a) {
+        const int slot = (a - t + A) % A;
+        const u64 bb = pk(bv[a], bv[a]);
+#pragma unroll
+        for (int c = 0; c < SC; ++c) {
+          const u64 q = mul2(bb, ring[slot][c]);
+          fma2(accA[a][c], flx[c], q);
+          fma2(accB[a][c], fly[c], q);
+        }
+      }
+    }
+  }
+}
+}  // namespace
+
+// MAXT bounds the CTA size: 256 threads keep at most two warps per SM
+// sub-partition, so up to 255 registers per thread; 384 allow more warps at
+// 168 registers.  The autotuner picks the variant per (N, S).
+template <bool TMA, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1)
+    calq32_kernel(int N, int S, int K2T, int NST, int NPL, const float *__restrict__ B32,
+                  const float2 *__restrict__ fin, float2 *__restrict__ Q) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const C32Geom g = c32_geom(N, K2T, NST, NPL);
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem);  // [MAX_ST]
+  uint64_t *empty = full + MAX_ST;                       // [MAX_ST]
+  uint64_t *pbar = full + 2 * MAX_ST;                    // [2] planes
+  float *Bs = reinterpret_cast<float *>(smem + g.off_B);
+  float2 *fls = reinterpret_cast<float2 *>(smem + g.off_fl);
+  float2 *plb = reinterpret_cast<float2 *>(smem + g.off_pl);
+  const long long NQ = (long long)N * N * N;
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int nwarps = (blockDim.x + 31) >> 5;
+  const int w = tid % WS;
+  const int rest = tid / WS;
+  const int r = rest % g.R;
+  const int k2l = rest / g.R;
+  const int k1 = blockIdx.y;
+  const int k2_0 = blockIdx.z * K2T;
+  const int k2n = min(K2T, N - k2_0);
+  const int k2 = k2_0 + k2l;
+  const bool k_ok = (k2l < k2n);
+  const int k2c = k_ok ? k2 : k2_0;
+  const int k3_0 = r * A;
+  const int s0 = blockIdx.x * SG;
+  const int nval = min(SG, S - s0);
+  const int NL = N * N;  // l-lines
+  const size_t plane_sz = (size_t)SG * g.PSTR;
+
+  // zero the tile/line buffers once: padded rows (l3 >= N), row tails and the
+  // f_l tails are never written by the copies and must read as zeros
+  {
+    const size_t nz = ((size_t)(g.off_pl - g.off_B)) / sizeof(float);
+    for (size_t e = tid; e < nz; e += blockDim.x) Bs[e] = 0.f;
+  }
+  if (tid == 0) {
+    for (int i = 0; i < MAX_ST; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], nwarps);
+    }
+    mbar_init(&pbar[0], 1);
+    mbar_init(&pbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  u64 accA[A][SC], accB[A][SC], hi[A][SC], lo[A][SC];  // packed (re, im)
+#pragma unroll
+  for (int a = 0; a < A; ++a)
+#pragma unroll
+    for (int c = 0; c < SC; ++c) {
+      accA[a][c] = 0ull;
+      accB[a][c] = 0ull;
+      hi[a][c] = 0ull;
+      lo[a][c] = 0ull;
+    }
+  const u64 neg_re = pk(-1.f, 1.f);
+
+  // prologue: lines 0 .. NST-2 and the first plane
+  int issued = 0, planes = 0;  // counted in warp 0
+  if (TMA && warp == 0) {
+    for (int li = 0; li < NST - 1 && li < NL; ++li, ++issued)
+      stage_line<true>(g, li, li % NST, k1, k2_0, k2n, s0, nval, NQ, B32, fin, Bs, fls, full);
+    stage_plane<true>(g, (k1 + N) % N, s0, nval, NQ, fin, plb, &pbar[0]);
+    ++planes;
+  }
+  bool to = false;
+  bool aborted = false;
+  for (int li = 0; li < NL; ++li) {
+    const int l1 = li / N, l2 = li % N;
+    const int st = li % NST;
+    const int pb = (NPL == 2) ? (l1 & 1) : 0;
+    if (l2 == 0) {
+      // every warp is done with plane l1-1 (and with its buffer)
+      if (__syncthreads_or(to)) {
+        aborted = true;
+        break;
+      }
+      if (TMA) {
+        if (NPL == 2) {
+          if (warp == 0 && l1 + 1 < N) {
+            stage_plane<true>(g, (k1 - (l1 + 1) + N) % N, s0, nval, NQ, fin,
+                              plb + (size_t)((l1 + 1) & 1) * plane_sz, &pbar[(l1 + 1) & 1]);
+            ++planes;
+          }
+          mbar_wait(&pbar[l1 & 1], (uint32_t)((l1 >> 1) & 1), to);
+        } else {
+          if (warp == 0 && l1 > 0) {
+            stage_plane<true>(g, (k1 - l1 + N) % N, s0, nval, NQ, fin, plb, &pbar[0]);
+            ++planes;
+          }
+          mbar_wait(&pbar[0], (uint32_t)(l1 & 1), to);
+        }
+      } else {
+        stage_plane<false>(g, (k1 - l1 + N) % N, s0, nval, NQ, fin, plb, pbar);
+      }
+    }
+    if (TMA) {
+      // refill: line li+NST-1 goes into the stage line li-1 used
+      const int ln = li + NST - 1;
+      if (warp == 0 && ln < NL) {
+        const int sn = ln % NST;
+        if (li >= 1) mbar_wait(&empty[sn], (uint32_t)(((li - 1) / NST) & 1), to);
+        stage_line<true>(g, ln, sn, k1, k2_0, k2n, s0, nval, NQ, B32, fin, Bs, fls, full);
+        ++issued;
+      }
+      mbar_wait(&full[st], (uint32_t)((li / NST) & 1), to);
+    } else {
+      __syncthreads();  // previous line's readers are done (single buffer)
+      stage_line<false>(g, li, st, k1, k2_0, k2n, s0, nval, NQ, B32, fin, Bs, fls, full);
+      __syncthreads();
+    }
+
+    // ---- compute line (l1, l2)
+    const int m2 = (k2c - l2 + N) % N;
+    const float *Bt = Bs + (size_t)st * g.RA * g.BROW + k2l * N + k3_0;
+    const float2 *fl0 = fls + (size_t)st * SG * g.FLS + (size_t)w * g.FLS;
+    const float2 *fl1 = fl0 + (size_t)WS * g.FLS;
+    const float2 *p0 = plb + (size_t)pb * plane_sz + (size_t)w * g.PSTR + m2 * N;
+    const float2 *p1 = p0 + (size_t)WS * g.PSTR;
+    if (TMA)
+      compute_line<true, true>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
+    else
+      compute_line<false, false>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
+    if (TMA) {
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[st]);
+    }
+    if ((l2 + 1) % FOLD_LINES == 0 || l2 == N - 1) {  // fold into the compensated pair
+#pragma unroll
+      for (int a = 0; a < A; ++a)
+#pragma unroll
+        for (int c = 0; c < SC; ++c) {
+          // (accA.x - accB.y, accA.y + accB.x) = accA + (-1, 1) * swap(accB)
+          const u64 x = fma2r(neg_re, swp(accB[a][c]), accA[a][c]);
+          two_sum_fold2(hi[a][c], lo[a][c], x);
+          accA[a][c] = 0ull;
+          accB[a][c] = 0ull;
+        }
+    }
+  }
+  if (!aborted && __syncthreads_or(to)) aborted = true;
+  if (aborted) {
+    if (tid == 0) {
+      atomicExch(&g_calq32_status, 1);
+      // drain: wait for the last phase issued on every barrier, so no copy
+      // lands after the block exits
+      bool t2 = false;
+      if (TMA) {
+        for (int sx = 0; sx < NST; ++sx) {
+          int last = -1;  // last line issued into stage sx
+          for (int x = issued - 1; x >= 0 && x >= issued - NST; --x)
+            if (x % NST == sx) last = x;
+          if (last >= 0) mbar_wait(&full[sx], (uint32_t)((last / NST) & 1), t2);
+        }
+        // plane x went to buffer (NPL == 2 ? x & 1 : 0); the last one issued into
+        // each buffer is the only phase that can still be pending there
+        for (int px = planes - NPL; px < planes; ++px) {
+          if (px < 0) continue;
+          const int b = (NPL == 2) ? (px & 1) : 0;
+          const int use = (NPL == 2) ? (px >> 1) : px;
+          mbar_wait(&pbar[b], (uint32_t)(use & 1), t2);
+        }
+      }
+    }
+    __syncthreads();
+    return;
+  }
+  if (!k_ok) return;
+#pragma unroll
+  for (int c = 0; c < SC; ++c) {
+    const int s = s0 + w + c * WS;
+    if (s >= S) continue;
+    float2 *qp = Q + (long long)s * NQ + (long long)k1 * N * N + (long long)k2 * N;
+#pragma unroll
+    for (int a = 0; a < A; ++a) {
+      const int k3 = k3_0 + a;
+      if (k3 < N) {
+        const float2 h = upk(hi[a][c]), l = upk(lo[a][c]);
+        qp[k3] = make_float2(h.x + l.x, h.y + l.y);
+      }
+    }
+  }
+}
+
+int calq32_variants() { return 2; }
+
+static int variant_maxt(int v) { return v == 0 ? 256 : 384; }
+
+template <bool TMA, int MAXT>
+static edb_status launch_c32(dim3 grid, int threads, size_t smem, int N, int S, int K2T, int NST,
+                             int NPL, const float *B32, const float2 *fin, float2 *Q,
+                             cudaStream_t st) {
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(calq32_kernel<TMA, MAXT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(calq32)");
+    configured = true;
+  }
+  calq32_kernel<TMA, MAXT><<<grid, threads, smem, st>>>(N, S, K2T, NST, NPL, B32, fin, Q);
+  EDB_LAUNCHED();
+  return EDB_OK;
+}
+
 edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin, float2 *d_Q,
-                               cudaStream_t st) {
+                               cudaStream_t st, int variant) {
+  if (variant < 0 || variant >= calq32_variants()) variant = 0;
+  const int maxt = variant_maxt(variant);
   const int R = (N + A - 1) / A;
-  int K2T = MAX_THREADS / (R * WS);
+  int K2T = maxt / (R * WS);
   if (K2T > N) K2T = N;
   if (K2T < 1) return fail(EDB_EINVAL, "calq32: N too large for the thread tile");
-  // balance the k2 tiles
-  int tiles = (N + K2T - 1) / K2T;
+  const int tiles = (N + K2T - 1) / K2T;
   K2T = (N + tiles - 1) / tiles;
   const int threads = K2T * R * WS;
-  size_t smem = (size_t)N * N * SG * sizeof(float2);
-  static int configured = 0;
-  if (!configured) {
-    EDB_CUDA(cudaFuncSetAttribute(calq32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  227 * 1024));
-    configured = 1;
+  // TMA bulk copies need 16-byte aligned sources: N % 4 == 0 makes every
+  // row/line/plane offset a multiple of 16 bytes; the base pointers are checked
+  const bool tma = (N % 4) == 0 && N >= A && ((uintptr_t)d_B32 % 16) == 0 &&
+                   ((uintptr_t)d_fin % 16) == 0;
+  // deepest pipeline that fits: two planes with >= 3 stages if possible,
+  // else one plane with up to MAX_ST stages (the plain path uses 1 + 1)
+  const size_t cap = 227 * 1024;
+  int NST = 1, NPL = 1;
+  if (tma) {
+    NST = 0;
+    for (int ns = MAX_ST; ns >= 3 && !NST; --ns)
+      if (c32_geom(N, K2T, ns, 2).bytes <= cap) {
+        NST = ns;
+        NPL = 2;
+      }
+    for (int ns = MAX_ST; ns >= 2 && !NST; --ns)
+      if (c32_geom(N, K2T, ns, 1).bytes <= cap) {
+        NST = ns;
+        NPL = 1;
+      }
+    if (!NST) return fail(EDB_EINVAL, "calq32: N too large for shared memory");
   }
-  if (smem > 227 * 1024) return fail(EDB_EINVAL, "calq32: N too large for shared memory");
+  const C32Geom g = c32_geom(N, K2T, NST, NPL);
+  if (g.bytes > cap) return fail(EDB_EINVAL, "calq32: N too large for shared memory");
   dim3 grid((unsigned)((S + SG - 1) / SG), (unsigned)N, (unsigned)tiles);
-  calq32_kernel<<<grid, threads, smem, st>>>(N, S, K2T, d_B32, d_fin, d_Q);
-  EDB_LAUNCHED();
+  if (tma)
+    return maxt == 256 ? launch_c32<true, 256>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
+                                               d_fin, d_Q, st)
+                       : launch_c32<true, 384>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
+                                               d_fin, d_Q, st);
+  return maxt == 256 ? launch_c32<false, 256>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
+                                              d_fin, d_Q, st)
+                     : launch_c32<false, 384>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
+                                              d_fin, d_Q, st);
+}
+
+edb_status read_calq32_status(int *status, bool clear) {
+  int v = 0;
+  EDB_CUDA(cudaMemcpyFromSymbol(&v, g_calq32_status, sizeof(int)));
+  if (clear && v) {
+    int z = 0;
+    EDB_CUDA(cudaMemcpyToSymbol(g_calq32_status, &z, sizeof(int)));
+  }
+  *status = v;
   return EDB_OK;
 }
 

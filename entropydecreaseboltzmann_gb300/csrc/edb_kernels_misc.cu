@@ -58,25 +58,35 @@ __device__ double mean_re(const double2 *F, const double *f, long long Nf, doubl
   return block_sum(acc, red) / (double)Nf;
 }
 
+// Block-uniform copy of the latched average (EntropyFix.h:20-22).  Thread 0
+// loads it from the per-solve state before a barrier and stores it back after
+// one, so no thread ever reads the state while another writes it.
+struct AvgSnap {
+  double avg;
+  int flag;
+};
+
 // FixSol (EntropyFix.h:268-309) on Re F (F != null, imaginary parts zeroed as
-// BKW.h:232 does) or on a real array f.  The bisection halves [betaL, betaR]
-// until its width is <= eps (about 34 halvings from [0,1] at eps = 1e-10),
-// so the loop is bounded; MAX_BISECT is a hard guard on top.
-__device__ void fixsol_dev(double2 *F, double *f, long long Nf, EfixState *st, double eps,
-                           double aim, double *red, double *shared_flag) {
+// BKW.h:232 does) or on a real array f.  `snap` lives in shared memory and is
+// block-uniform on entry and exit.  The bisection halves [betaL, betaR] until
+// its width is <= eps (about 34 halvings from [0,1] at eps = 1e-10), so the
+// loop is bounded; MAX_BISECT is a hard guard on top.  Every branch below
+// depends only on block-reduced values, so all threads take it together.
+__device__ void fixsol_dev(double2 *F, double *f, long long Nf, AvgSnap *snap, double eps,
+                           double aim, double *red) {
   const int MAX_BISECT = 400;
   double betaL = 0.0, betaR = 1.0;
   for (int it = 0; it < MAX_BISECT && (betaR - betaL) > eps; ++it) {
     double betaMid = 0.5 * (betaL + betaR);
-    if (!st->avg_flag) {
-      double avg = mean_re(F, f, Nf, red);
+    if (!snap->flag) {
+      double avg = mean_re(F, f, Nf, red);  // ends with a barrier
       if (threadIdx.x == 0) {
-        st->avg = avg;
-        st->avg_flag = 1;
+        snap->avg = avg;
+        snap->flag = 1;
       }
       __syncthreads();
     }
-    const double avg = st->avg;
+    const double avg = snap->avg;
     const double betaFbar = betaMid * avg;
     const double omb = 1. - betaMid;
     double s = efix_sum(F, f, Nf, betaFbar, omb, true, eps, red);
@@ -99,7 +109,7 @@ __device__ void fixsol_dev(double2 *F, double *f, long long Nf, EfixState *st, d
     else
       betaL = betaMid;
   }
-  const double betaFbar = betaR * st->avg;
+  const double betaFbar = betaR * snap->avg;
   for (long long i = threadIdx.x; i < Nf; i += blockDim.x) {
     double x = F ? F[i].x : f[i];
     x *= (1.0 - betaR);
@@ -110,7 +120,6 @@ __device__ void fixsol_dev(double2 *F, double *f, long long Nf, EfixState *st, d
       f[i] = x;
   }
   __syncthreads();
-  (void)shared_flag;
 }
 }  // namespace
 
@@ -145,29 +154,40 @@ __global__ void __launch_bounds__(RT)
                         double *__restrict__ trace_raw, double *__restrict__ trace_fixed,
                         int trace_cap) {
   __shared__ double red[RT];
-  __shared__ double flag;
+  __shared__ AvgSnap snap;
+  __shared__ double H_prev;
+  __shared__ int step, rec;
   double2 *Fs = F + (long long)blockIdx.x * NQ;
   EfixState *st = state + blockIdx.x;
+  if (threadIdx.x == 0) {
+    snap.avg = st->avg;
+    snap.flag = st->avg_flag;
+    H_prev = st->H_prev;
+    step = st->step;
+    rec = st->rec;
+  }
+  __syncthreads();
   double acc = 0.0;
   for (long long i = threadIdx.x; i < NQ; i += blockDim.x) acc += flogf_dev(Fs[i].x);
   double H = block_sum(acc, red) * vol;
   const double raw = H;
-  const int step = st->step;
   bool allowed = false;
   if (fix_mode == 1) allowed = step > 1;
   else if (fix_mode == 2) allowed = step != 0;
-  if (allowed && H - st->H_prev > 1.0e-10) {
-    fixsol_dev(Fs, nullptr, NQ, st, eps, st->H_prev / R3, red, &flag);
+  if (allowed && H - H_prev > 1.0e-10) {
+    fixsol_dev(Fs, nullptr, NQ, &snap, eps, H_prev / R3, red);
     double acc2 = 0.0;
     for (long long i = threadIdx.x; i < NQ; i += blockDim.x) acc2 += flogf_dev(Fs[i].x);
     H = block_sum(acc2, red) * vol;
   }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    const int rec = st->rec;
     if (rec < trace_cap) {
       trace_raw[(long long)blockIdx.x * trace_cap + rec] = raw;
       trace_fixed[(long long)blockIdx.x * trace_cap + rec] = H;
     }
+    st->avg = snap.avg;
+    st->avg_flag = snap.flag;
     st->rec = rec + 1;
     st->H_prev = H;
     st->step = step + 1;
@@ -201,23 +221,42 @@ __global__ void __launch_bounds__(RT) efix_entropy_kernel(long long Nf, const do
                                                           EfixState *st, double eps,
                                                           double *H) {
   __shared__ double red[RT];
-  if (!st->avg_flag) {
-    double avg = mean_re(nullptr, f, Nf, red);
+  __shared__ AvgSnap snap;
+  if (threadIdx.x == 0) {
+    snap.avg = st->avg;
+    snap.flag = st->avg_flag;
+  }
+  __syncthreads();
+  if (!snap.flag) {
+    double avg = mean_re(nullptr, f, Nf, red);  // ends with a barrier
     if (threadIdx.x == 0) {
-      st->avg = avg;
-      st->avg_flag = 1;
+      snap.avg = avg;
+      snap.flag = 1;
     }
     __syncthreads();
   }
   double s = efix_sum(nullptr, f, Nf, 0.0, 1.0, false, eps, red);
-  if (threadIdx.x == 0) *H = s / (double)Nf - st->avg;
+  if (threadIdx.x == 0) {
+    *H = s / (double)Nf - snap.avg;
+    st->avg = snap.avg;
+    st->avg_flag = snap.flag;
+  }
 }
 
 __global__ void __launch_bounds__(RT) efix_fixsol_kernel(long long Nf, double *f, EfixState *st,
                                                          double eps, double aim) {
   __shared__ double red[RT];
-  __shared__ double flag;
-  fixsol_dev(nullptr, f, Nf, st, eps, aim, red, &flag);
+  __shared__ AvgSnap snap;
+  if (threadIdx.x == 0) {
+    snap.avg = st->avg;
+    snap.flag = st->avg_flag;
+  }
+  __syncthreads();
+  fixsol_dev(nullptr, f, Nf, &snap, eps, aim, red);
+  if (threadIdx.x == 0) {
+    st->avg = snap.avg;
+    st->avg_flag = snap.flag;
+  }
 }
 
 edb_status launch_efix_average(int Nf, const double *d_f, EfixState *d_state, cudaStream_t st) {

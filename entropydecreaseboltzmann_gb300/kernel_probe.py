@@ -39,6 +39,8 @@ def main():
         fh = np.fft.fftn(F0.reshape(S, N, N, N), axes=(1, 2, 3)).reshape(S, -1)
         fin = torch.from_numpy(fh.astype(np.complex64)).cuda()
         out = torch.empty_like(fin)
+        v = q.autotune_batch(S, fin, out, stream)  # 3 launches per variant
+        print(f"autotuned variant {v}")
         run = lambda: q.calQ_batch_f32(S, fin, out, stream)  # noqa: E731
         terms = float(N) ** 6 * S
     else:
@@ -58,6 +60,17 @@ def main():
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.reps
+    if args.kernel == "calq32":
+        ref = out.clone()
+        torch.cuda.synchronize()
+        st = edb.device_status(clear=True)
+        print(f"device status {st}, finite {bool(torch.isfinite(torch.view_as_real(ref)).all())}")
+    import ctypes as C
+
+    p1, p2 = C.c_double(), C.c_double()
+    edb.lib.edb_measure_fp32_peak(C.byref(p1))
+    edb.lib.edb_measure_fp32x2_peak(C.byref(p2))
+    print(f"FP32 FMA peak probe: scalar {p1.value:.1f} TFLOP/s, packed f32x2 {p2.value:.1f} TFLOP/s")
     print(f"{args.kernel} N={N} S={S}: {ms:.3f} ms/launch, "
           f"{10 * terms / (ms * 1e-3) / 1e12:.2f} TFLOP/s (10 flop/term)")
 

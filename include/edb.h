@@ -76,6 +76,8 @@ long long edb_kernel_launch_count(void);
  * probe kernel); the denominator of the batched kernel's roofline fraction.
  * No reference counterpart (the reference has no GPU code). */
 edb_status edb_measure_fp32_peak(double *tflops);
+/* Same with packed fma.rn.f32x2 instructions (two FP32 FMAs each). */
+edb_status edb_measure_fp32x2_peak(double *tflops);
 
 /* ------------------------------------------------------------ QCalculator */
 
@@ -139,6 +141,18 @@ edb_status edb_qcalc_calQ_batch_f32_device(edb_qcalc *q, int S, const float *d_f
  * Calls that overlap on the GPU share the array and race: serialise them. */
 edb_status edb_calQ_fp64_noalloc(int N, int index_mode, const double *d_B, const double *d_fin,
                                  double *d_Qout, void *stream);
+
+/* Autotuner of the batched kernel (no reference counterpart): times each
+ * launch variant (CTA size / k2-tile shape) on the caller's buffers and keeps
+ * the fastest for S's size class; later batched calls on this handle use it.
+ * edb_batch_load* runs it once per size class before the step graph is built. */
+edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float *d_fin, float *d_Qout,
+                                    void *stream, int *chosen);
+
+/* Device status word of the batched kernel: nonzero when one of its bounded
+ * waits ran out (the launch then returned early and its output is invalid).
+ * clear != 0 resets it.  No reference counterpart. */
+edb_status edb_device_status(int *status, int clear);
 
 /* Copies count entries of the FP64 B table starting at flat index first
  * (row-major [l][k], centred indices) to host memory. */
