@@ -22,6 +22,7 @@ INDEX_REFERENCE = 0
 INDEX_ALIASED = 1
 R_REFERENCE = 6.62132
 SCHEME_FE, SCHEME_CFE, SCHEME_RK2, SCHEME_SSP3, SCHEME_RK4, SCHEME_DUFORT = range(6)
+FP64_EMULATED, FP64_NATIVE = 0, 1
 
 
 class EdbError(RuntimeError):
@@ -79,6 +80,7 @@ def _load():
         "edb_qcalc_calQ_batch_f32_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
         "edb_qcalc_autotune_batch": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _ip]),
         "edb_device_status": (C.c_int, [_ip, C.c_int]),
+        "edb_qcalc_set_fp64_kernel": (C.c_int, [_vp, C.c_int]),
         "edb_qcalc_copy_B": (C.c_int, [_vp, C.c_longlong, C.c_longlong, _dp]),
         "edb_qcalc_set_B": (C.c_int, [_vp, _dp]),
         "edb_qcalc_get_info": (C.c_int, [_vp, C.POINTER(QCalcInfo)]),

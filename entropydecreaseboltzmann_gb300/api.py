@@ -90,6 +90,10 @@ class QCalculator:
         check(lib.edb_qcalc_calQ_batch_f32_device(self._h, int(S), devptr(d_fin), devptr(d_Q),
                                                   stream_ptr(stream)))
 
+    def set_fp64_kernel(self, kind):
+        """0 = FP64-accurate double-float on the FP32 pipe (default), 1 = native FP64."""
+        check(lib.edb_qcalc_set_fp64_kernel(self._h, int(kind)))
+
     def autotune_batch(self, S, d_fin, d_Q, stream=None):
         """Pick the fastest batched-kernel variant for S solves; returns its index."""
         v = C.c_int()

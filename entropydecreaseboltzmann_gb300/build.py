@@ -25,6 +25,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "edb_capi.cu": [],
     "edb_kernels_calq.cu": [],
+    "edb_kernels_calq64x.cu": [],
     "edb_kernels_fft.cu": [],
     "edb_kernels_genb.cu": ["-fmad=false"],
     "edb_kernels_misc.cu": ["-fmad=false"],

@@ -86,8 +86,11 @@ struct edb_qcalc {
   edb_qcalc_desc d;
   QParams p;
   cudaStream_t st = nullptr;
-  double *B64 = nullptr;    // [l][k] centred, N^3 x KC... stored N^3 x N^3
+  double *B64 = nullptr;    // [l][k] centred, N^3 x N^3 (flat stream of row stride KC)
+  float2 *B2 = nullptr;     // B64 split into (hi, lo) floats, same layout
   float *B32 = nullptr;     // FFTW order [l][k] (ALIASED only)
+  float4 *fdf = nullptr;    // input split for the double-float kernel
+  int fp64_kernel = EDB_FP64_EMULATED;
   double2 *partial = nullptr;
   double2 *fin = nullptr, *Q = nullptr;  // host-API staging
   int nchunk = 0;
@@ -151,7 +154,9 @@ extern "C" edb_status edb_qcalc_destroy(edb_qcalc *q) {
   if (!q) return EDB_OK;
   if (q->st) cudaStreamSynchronize(q->st);
   dfree(q->B64);
+  dfree(q->B2);
   dfree(q->B32);
+  dfree(q->fdf);
   dfree(q->partial);
   dfree(q->fin);
   dfree(q->Q);
@@ -176,8 +181,10 @@ static int amax_of(int N) {
 static edb_status qcalc_alloc_work(edb_qcalc *q) {
   if (!q->partial) {
     q->nchunk = calq64_nchunk(q->p);
-    EDB_TRY(dalloc(&q->partial, (size_t)q->nchunk * q->p.KC));
+    const int nx = calq64x_nchunk(q->p, nullptr);
+    EDB_TRY(dalloc(&q->partial, (size_t)(q->nchunk > nx ? q->nchunk : nx) * q->p.KC));
   }
+  if (!q->fdf) EDB_TRY(dalloc(&q->fdf, (size_t)q->p.NQ));
   if (!q->fin) EDB_TRY(dalloc(&q->fin, (size_t)q->p.NQ));
   if (!q->Q) EDB_TRY(dalloc(&q->Q, (size_t)q->p.NQ));
   return EDB_OK;
@@ -191,6 +198,7 @@ extern "C" edb_status edb_qcalc_genB(edb_qcalc *q) {
   double *T = nullptr, *sigma = nullptr, *Bmm = nullptr;
   edb_status s = EDB_OK;
   if (!q->B64) EDB_TRY(dalloc(&q->B64, (size_t)NQ * NQ));
+  if (!q->B2) EDB_TRY(dalloc(&q->B2, (size_t)NQ * NQ));
   if (q->d.index_mode == EDB_INDEX_ALIASED && !q->B32)
     EDB_TRY(dalloc(&q->B32, (size_t)NQ * NQ + 64));  // +64: masked tail reads of calq32
   EDB_TRY(qcalc_alloc_work(q));
@@ -204,6 +212,7 @@ extern "C" edb_status edb_qcalc_genB(edb_qcalc *q) {
   if (s == EDB_OK)
     s = launch_genB(N, q->d.gamma, q->d.L, q->d.filter, q->d.index_mode, T, amax, sigma, Bmm,
                     q->B64, q->B32, q->st);
+  if (s == EDB_OK) s = launch_split_B(NQ * NQ, q->B64, q->B2, q->st);
   cudaError_t e = cudaStreamSynchronize(q->st);
   dfree(T);
   dfree(sigma);
@@ -220,6 +229,9 @@ extern "C" edb_status edb_qcalc_set_B(edb_qcalc *q, const double *host_B) {
   if (!q->B64) EDB_TRY(dalloc(&q->B64, (size_t)NQ * NQ));
   EDB_TRY(qcalc_alloc_work(q));
   EDB_CUDA(cudaMemcpy(q->B64, host_B, sizeof(double) * NQ * NQ, cudaMemcpyHostToDevice));
+  if (!q->B2) EDB_TRY(dalloc(&q->B2, (size_t)NQ * NQ));
+  EDB_TRY(launch_split_B(NQ * NQ, q->B64, q->B2, q->st));
+  EDB_CUDA(cudaStreamSynchronize(q->st));
   dfree(q->B32);  // the FP32 copy no longer matches
   q->ready = true;
   return EDB_OK;
@@ -247,12 +259,27 @@ extern "C" edb_status edb_qcalc_get_info(edb_qcalc *q, edb_qcalc_info *out) {
   return EDB_OK;
 }
 
+// The FP64 collision sum with the handle's selected kernel.
+static edb_status qcalc_fp64(edb_qcalc *q, const double2 *in, double2 *out, cudaStream_t st) {
+  if (q->fp64_kernel == EDB_FP64_EMULATED && q->B2) {
+    EDB_TRY(launch_split_f(q->p.NQ, in, q->fdf, st));
+    return launch_calq64x(q->p, q->B2, q->fdf, q->partial, out, st);
+  }
+  return launch_calq64(q->p, q->B64, in, q->partial, out, st);
+}
+
+extern "C" edb_status edb_qcalc_set_fp64_kernel(edb_qcalc *q, int kind) {
+  if (!q) return fail(EDB_EINVAL, "null handle");
+  if (kind != EDB_FP64_EMULATED && kind != EDB_FP64_NATIVE) return fail(EDB_EINVAL, "unknown kind");
+  q->fp64_kernel = kind;
+  return EDB_OK;
+}
+
 extern "C" edb_status edb_qcalc_calQ_device(edb_qcalc *q, const double *d_fin, double *d_Qout,
                                             void *stream) {
   if (!q || !d_fin || !d_Qout) return fail(EDB_EINVAL, "null argument");
   if (!q->ready) return fail(EDB_ENOTREADY, "calQ before genB");
-  return launch_calq64(q->p, q->B64, (const double2 *)d_fin, q->partial, (double2 *)d_Qout,
-                       (cudaStream_t)stream);
+  return qcalc_fp64(q, (const double2 *)d_fin, (double2 *)d_Qout, (cudaStream_t)stream);
 }
 
 extern "C" edb_status edb_qcalc_calQ(edb_qcalc *q, const double *fin, double *Qout) {
@@ -260,7 +287,7 @@ extern "C" edb_status edb_qcalc_calQ(edb_qcalc *q, const double *fin, double *Qo
   if (!q->ready) return fail(EDB_ENOTREADY, "calQ before genB");
   const size_t bytes = sizeof(double2) * q->p.NQ;
   EDB_CUDA(cudaMemcpyAsync(q->fin, fin, bytes, cudaMemcpyHostToDevice, q->st));
-  EDB_TRY(launch_calq64(q->p, q->B64, q->fin, q->partial, q->Q, q->st));
+  EDB_TRY(qcalc_fp64(q, q->fin, q->Q, q->st));
   EDB_CUDA(cudaMemcpyAsync(Qout, q->Q, bytes, cudaMemcpyDeviceToHost, q->st));
   EDB_CUDA(cudaStreamSynchronize(q->st));
   return EDB_OK;
@@ -294,6 +321,10 @@ extern "C" edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float 
   edb_status rc = EDB_OK;
   for (int v = 0; v < calq32_variants() && rc == EDB_OK; ++v) {
     rc = launch_calq32_batch(q->d.N, S, q->B32, (const float2 *)d_fin, (float2 *)d_Qout, st, v);
+    if (rc == EDB_EINVAL) {  // this variant does not fit this N: skip it
+      rc = EDB_OK;
+      continue;
+    }
     if (rc != EDB_OK) break;
     cudaEventRecord(e0, st);
     for (int r = 0; r < 2 && rc == EDB_OK; ++r)
@@ -545,9 +576,7 @@ static edb_status solver_step(edb_solver *s, double dt, bool dufort_startup) {
   cudaStream_t st = s->st;
   edb_qcalc *q = s->q;
   double2 *Fh = s->Fhat, **Q = s->Qs, **F = s->Fs;
-  auto calq = [&](const double2 *in, double2 *out) {
-    return launch_calq64(q->p, q->B64, in, q->partial, out, st);
-  };
+  auto calq = [&](const double2 *in, double2 *out) { return qcalc_fp64(q, in, out, st); };
   switch (s->d.scheme) {
     case EDB_SCHEME_FE:  // BKW.h:220-222
       EDB_TRY(calq(Fh, Q[0]));

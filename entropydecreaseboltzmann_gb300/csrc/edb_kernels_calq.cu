@@ -138,6 +138,16 @@ edb_status launch_calq64(const QParams &p, const double *d_B, const double2 *d_f
   return EDB_OK;
 }
 
+// The ordered chunk reduction and output permutation alone, for the
+// double-float kernel (edb_kernels_calq64x.cu), which writes the same partial
+// layout.
+edb_status launch_calq64_reduce(const QParams &p, int nchunk, const double2 *d_partial,
+                                double2 *d_Q, cudaStream_t st) {
+  calq64_reduce_kernel<<<(unsigned)((p.NQ + 255) / 256), 256, 0, st>>>(p, nchunk, d_partial, d_Q);
+  EDB_LAUNCHED();
+  return EDB_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Batched FP32 kernel (ALIASED mode, many solves sharing one table).
 //
@@ -188,13 +198,15 @@ __device__ int g_calq32_status;  // nonzero: a bounded wait ran out
 constexpr int MAX_ST = 4;                 // pipeline stages (l-lines in flight)
 
 struct C32Geom {
-  int N, R, RA, K2T, BROW, FLS, PSTR, NST, NPL;
-  size_t off_B, off_fl, off_pl, bytes;
+  int N, R, RA, K2T, BROW, FLS, PSTR, NST, NPL, HLT;
+  size_t off_B, off_fl, off_pl, off_hl, bytes;
 };
 
 // Shared-memory layout for a CTA: NST stages of (B tile, f_l lines), NPL
-// m1-planes.  Barriers: full[MAX_ST], empty[MAX_ST], plane[2].
-__host__ __device__ inline C32Geom c32_geom(int N, int K2T, int NST, int NPL) {
+// m1-planes and, when HLT > 0, the compensated (hi, lo) sums of HLT threads
+// (2 * A * SC packed pairs each, thread-fastest so accesses never conflict).
+// Barriers: full[MAX_ST], empty[MAX_ST], plane[2].
+__host__ __device__ inline C32Geom c32_geom(int N, int K2T, int NST, int NPL, int HLT) {
   C32Geom g;
   g.N = N;
   g.R = (N + A - 1) / A;
@@ -202,6 +214,7 @@ __host__ __device__ inline C32Geom c32_geom(int N, int K2T, int NST, int NPL) {
   g.K2T = K2T;
   g.NST = NST;
   g.NPL = NPL;
+  g.HLT = HLT;
   g.BROW = K2T * N + ROWPAD;
   g.FLS = g.RA + FLPAD;
   g.PSTR = N * N + PLPAD;
@@ -212,6 +225,8 @@ __host__ __device__ inline C32Geom c32_geom(int N, int K2T, int NST, int NPL) {
   o += sizeof(float2) * (size_t)NST * SG * g.FLS;
   g.off_pl = o;
   o += sizeof(float2) * (size_t)NPL * SG * g.PSTR;
+  g.off_hl = o;
+  o += sizeof(unsigned long long) * 2 * A * SC * (size_t)HLT;
   g.bytes = o;
   return g;
 }
@@ -459,12 +474,14 @@ __device__ __forceinline__ void compute_line(const C32Geom &g, const float *Bt, 
 // MAXT bounds the CTA size: 256 threads keep at most two warps per SM
 // sub-partition, so up to 255 registers per thread; 384 allow more warps at
 // 168 registers.  The autotuner picks the variant per (N, S).
-template <bool TMA, int MAXT>
+// HLS: keep the compensated (hi, lo) pairs in shared memory instead of
+// registers, which frees 64 registers per thread for more resident warps.
+template <bool TMA, int MAXT, bool HLS>
 __global__ void __launch_bounds__(MAXT, 1)
     calq32_kernel(int N, int S, int K2T, int NST, int NPL, const float *__restrict__ B32,
                   const float2 *__restrict__ fin, float2 *__restrict__ Q) {
   extern __shared__ __align__(128) unsigned char smem[];
-  const C32Geom g = c32_geom(N, K2T, NST, NPL);
+  const C32Geom g = c32_geom(N, K2T, NST, NPL, HLS ? (int)blockDim.x : 0);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);  // [MAX_ST]
   uint64_t *empty = full + MAX_ST;                       // [MAX_ST]
   uint64_t *pbar = full + 2 * MAX_ST;                    // [2] planes
@@ -508,15 +525,22 @@ __global__ void __launch_bounds__(MAXT, 1)
   }
   __syncthreads();
 
-  u64 accA[A][SC], accB[A][SC], hi[A][SC], lo[A][SC];  // packed (re, im)
+  u64 accA[A][SC], accB[A][SC];            // packed (re, im) partial sums
+  u64 hi[HLS ? 1 : A][SC], lo[HLS ? 1 : A][SC];  // compensated sums (registers)
+  u64 *hl = reinterpret_cast<u64 *>(smem + g.off_hl);  // or [2*A*SC][threads] in smem
 #pragma unroll
   for (int a = 0; a < A; ++a)
 #pragma unroll
     for (int c = 0; c < SC; ++c) {
       accA[a][c] = 0ull;
       accB[a][c] = 0ull;
-      hi[a][c] = 0ull;
-      lo[a][c] = 0ull;
+      if (HLS) {
+        hl[(size_t)(2 * (a * SC + c)) * blockDim.x + tid] = 0ull;
+        hl[(size_t)(2 * (a * SC + c) + 1) * blockDim.x + tid] = 0ull;
+      } else {
+        hi[HLS ? 0 : a][c] = 0ull;
+        lo[HLS ? 0 : a][c] = 0ull;
+      }
     }
   const u64 neg_re = pk(-1.f, 1.f);
 
@@ -597,7 +621,15 @@ __global__ void __launch_bounds__(MAXT, 1)
         for (int c = 0; c < SC; ++c) {
           // (accA.x - accB.y, accA.y + accB.x) = accA + (-1, 1) * swap(accB)
           const u64 x = fma2r(neg_re, swp(accB[a][c]), accA[a][c]);
-          two_sum_fold2(hi[a][c], lo[a][c], x);
+          if (HLS) {
+            u64 *ph = hl + (size_t)(2 * (a * SC + c)) * blockDim.x + tid;
+            u64 h = ph[0], l = ph[blockDim.x];
+            two_sum_fold2(h, l, x);
+            ph[0] = h;
+            ph[blockDim.x] = l;
+          } else {
+            two_sum_fold2(hi[HLS ? 0 : a][c], lo[HLS ? 0 : a][c], x);
+          }
           accA[a][c] = 0ull;
           accB[a][c] = 0ull;
         }
@@ -640,29 +672,40 @@ __global__ void __launch_bounds__(MAXT, 1)
     for (int a = 0; a < A; ++a) {
       const int k3 = k3_0 + a;
       if (k3 < N) {
-        const float2 h = upk(hi[a][c]), l = upk(lo[a][c]);
+        u64 hv, lv;
+        if (HLS) {
+          hv = hl[(size_t)(2 * (a * SC + c)) * blockDim.x + tid];
+          lv = hl[(size_t)(2 * (a * SC + c) + 1) * blockDim.x + tid];
+        } else {
+          hv = hi[HLS ? 0 : a][c];
+          lv = lo[HLS ? 0 : a][c];
+        }
+        const float2 h = upk(hv), l = upk(lv);
         qp[k3] = make_float2(h.x + l.x, h.y + l.y);
       }
     }
   }
 }
 
+// Variants the autotuner chooses from:
+//   0: CTA <= 256 threads, (hi, lo) in registers (up to 255 registers/thread)
+//   1: CTA <= 384 threads, (hi, lo) in shared memory (168 registers/thread)
 int calq32_variants() { return 2; }
 
 static int variant_maxt(int v) { return v == 0 ? 256 : 384; }
 
-template <bool TMA, int MAXT>
+template <bool TMA, int MAXT, bool HLS>
 static edb_status launch_c32(dim3 grid, int threads, size_t smem, int N, int S, int K2T, int NST,
                              int NPL, const float *B32, const float2 *fin, float2 *Q,
                              cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(calq32_kernel<TMA, MAXT>,
+    cudaError_t e = cudaFuncSetAttribute(calq32_kernel<TMA, MAXT, HLS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(calq32)");
     configured = true;
   }
-  calq32_kernel<TMA, MAXT><<<grid, threads, smem, st>>>(N, S, K2T, NST, NPL, B32, fin, Q);
+  calq32_kernel<TMA, MAXT, HLS><<<grid, threads, smem, st>>>(N, S, K2T, NST, NPL, B32, fin, Q);
   EDB_LAUNCHED();
   return EDB_OK;
 }
@@ -671,6 +714,7 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
                                cudaStream_t st, int variant) {
   if (variant < 0 || variant >= calq32_variants()) variant = 0;
   const int maxt = variant_maxt(variant);
+  const bool hls = variant == 1;
   const int R = (N + A - 1) / A;
   int K2T = maxt / (R * WS);
   if (K2T > N) K2T = N;
@@ -678,6 +722,7 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   const int tiles = (N + K2T - 1) / K2T;
   K2T = (N + tiles - 1) / tiles;
   const int threads = K2T * R * WS;
+  const int hlt = hls ? threads : 0;
   // TMA bulk copies need 16-byte aligned sources: N % 4 == 0 makes every
   // row/line/plane offset a multiple of 16 bytes; the base pointers are checked
   const bool tma = (N % 4) == 0 && N >= A && ((uintptr_t)d_B32 % 16) == 0 &&
@@ -689,29 +734,29 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   if (tma) {
     NST = 0;
     for (int ns = MAX_ST; ns >= 3 && !NST; --ns)
-      if (c32_geom(N, K2T, ns, 2).bytes <= cap) {
+      if (c32_geom(N, K2T, ns, 2, hlt).bytes <= cap) {
         NST = ns;
         NPL = 2;
       }
     for (int ns = MAX_ST; ns >= 2 && !NST; --ns)
-      if (c32_geom(N, K2T, ns, 1).bytes <= cap) {
+      if (c32_geom(N, K2T, ns, 1, hlt).bytes <= cap) {
         NST = ns;
         NPL = 1;
       }
-    if (!NST) return fail(EDB_EINVAL, "calq32: N too large for shared memory");
+    if (!NST) return fail(EDB_EINVAL, "calq32: this variant does not fit in shared memory");
   }
-  const C32Geom g = c32_geom(N, K2T, NST, NPL);
-  if (g.bytes > cap) return fail(EDB_EINVAL, "calq32: N too large for shared memory");
+  const C32Geom g = c32_geom(N, K2T, NST, NPL, hlt);
+  if (g.bytes > cap) return fail(EDB_EINVAL, "calq32: this variant does not fit in shared memory");
   dim3 grid((unsigned)((S + SG - 1) / SG), (unsigned)N, (unsigned)tiles);
   if (tma)
-    return maxt == 256 ? launch_c32<true, 256>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
-                                               d_fin, d_Q, st)
-                       : launch_c32<true, 384>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
-                                               d_fin, d_Q, st);
-  return maxt == 256 ? launch_c32<false, 256>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
-                                              d_fin, d_Q, st)
-                     : launch_c32<false, 384>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
+    return hls ? launch_c32<true, 384, true>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
+                                             d_fin, d_Q, st)
+               : launch_c32<true, 256, false>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
                                               d_fin, d_Q, st);
+  return hls ? launch_c32<false, 384, true>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
+                                            d_fin, d_Q, st)
+             : launch_c32<false, 256, false>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
+                                             d_fin, d_Q, st);
 }
 
 edb_status read_calq32_status(int *status, bool clear) {

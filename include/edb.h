@@ -154,6 +154,15 @@ edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float *d_fin, flo
  * clear != 0 resets it.  No reference counterpart. */
 edb_status edb_device_status(int *status, int clear);
 
+/* Kernel of the FP64 collision sum (edb_qcalc_calQ, _device, the integrator).
+ * EMULATED (default): FP64-accurate double-float arithmetic on the FP32 pipe,
+ * reading the table pre-split into (hi, lo) floats (8 bytes per term, like
+ * FP64); GB300's native FP64 rate would hold the B stream near a tenth of HBM
+ * bandwidth.  NATIVE: the same sum with FP64 FMA.  No reference counterpart. */
+#define EDB_FP64_EMULATED 0
+#define EDB_FP64_NATIVE 1
+edb_status edb_qcalc_set_fp64_kernel(edb_qcalc *q, int kind);
+
 /* Copies count entries of the FP64 B table starting at flat index first
  * (row-major [l][k], centred indices) to host memory. */
 edb_status edb_qcalc_copy_B(edb_qcalc *q, long long first, long long count, double *host_out);
