@@ -91,6 +91,7 @@ struct edb_qcalc {
   float *B32 = nullptr;     // FFTW order [l][k] (ALIASED only)
   float4 *fdf = nullptr;    // input split for the double-float kernel
   int fp64_kernel = EDB_FP64_EMULATED;
+  int c64x_minb = 2;    // register cap of the double-float kernel, tuned at genB
   double2 *partial = nullptr;
   double2 *fin = nullptr, *Q = nullptr;  // host-API staging
   int nchunk = 0;
@@ -181,13 +182,53 @@ static int amax_of(int N) {
 static edb_status qcalc_alloc_work(edb_qcalc *q) {
   if (!q->partial) {
     q->nchunk = calq64_nchunk(q->p);
-    const int nx = calq64x_nchunk(q->p, nullptr);
-    EDB_TRY(dalloc(&q->partial, (size_t)(q->nchunk > nx ? q->nchunk : nx) * q->p.KC));
+    int nmax = calq64x_nchunk(q->p, nullptr);
+    if (q->nchunk > nmax) nmax = q->nchunk;
+    EDB_TRY(dalloc(&q->partial, (size_t)nmax * q->p.KC));
   }
-  if (!q->fdf) EDB_TRY(dalloc(&q->fdf, (size_t)q->p.NQ));
+
+  if (!q->fdf) EDB_TRY(dalloc(&q->fdf, (size_t)q->p.NQ));  // split f
   if (!q->fin) EDB_TRY(dalloc(&q->fin, (size_t)q->p.NQ));
   if (!q->Q) EDB_TRY(dalloc(&q->Q, (size_t)q->p.NQ));
   return EDB_OK;
+}
+
+// Times both register caps of the double-float kernel on this table (input:
+// the zeroed staging buffer; the kernel's cost does not depend on the values)
+// and keeps the faster.
+static edb_status qcalc_tune_fp64(edb_qcalc *q) {
+  if (!q->B2) return EDB_OK;
+  cudaStream_t st = q->st;
+  EDB_CUDA(cudaMemsetAsync(q->fin, 0, sizeof(double2) * q->p.NQ, st));
+  EDB_TRY(launch_split_f(q->p.NQ, q->fin, q->fdf, st));
+  cudaEvent_t e0, e1;
+  EDB_CUDA(cudaEventCreate(&e0));
+  EDB_CUDA(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int best_minb = 2;
+  edb_status rc = EDB_OK;
+  for (int minb = 2; minb >= 1 && rc == EDB_OK; --minb) {
+    rc = launch_calq64x(q->p, q->B2, q->fdf, q->partial, q->Q, st, minb);
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < 2 && rc == EDB_OK; ++r)
+      rc = launch_calq64x(q->p, q->B2, q->fdf, q->partial, q->Q, st, minb);
+    cudaEventRecord(e1, st);
+    cudaError_t ce = cudaEventSynchronize(e1);
+    if (ce != cudaSuccess) {
+      rc = cuda_fail(ce, "fp64 tune");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      best_minb = minb;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  q->c64x_minb = best_minb;
+  return rc;
 }
 
 extern "C" edb_status edb_qcalc_genB(edb_qcalc *q) {
@@ -220,7 +261,7 @@ extern "C" edb_status edb_qcalc_genB(edb_qcalc *q) {
   if (s != EDB_OK) return s;
   if (e != cudaSuccess) return cuda_fail(e, "genB");
   q->ready = true;
-  return EDB_OK;
+  return qcalc_tune_fp64(q);
 }
 
 extern "C" edb_status edb_qcalc_set_B(edb_qcalc *q, const double *host_B) {
@@ -234,7 +275,7 @@ extern "C" edb_status edb_qcalc_set_B(edb_qcalc *q, const double *host_B) {
   EDB_CUDA(cudaStreamSynchronize(q->st));
   dfree(q->B32);  // the FP32 copy no longer matches
   q->ready = true;
-  return EDB_OK;
+  return qcalc_tune_fp64(q);
 }
 
 extern "C" edb_status edb_qcalc_copy_B(edb_qcalc *q, long long first, long long count,
@@ -263,7 +304,7 @@ extern "C" edb_status edb_qcalc_get_info(edb_qcalc *q, edb_qcalc_info *out) {
 static edb_status qcalc_fp64(edb_qcalc *q, const double2 *in, double2 *out, cudaStream_t st) {
   if (q->fp64_kernel == EDB_FP64_EMULATED && q->B2) {
     EDB_TRY(launch_split_f(q->p.NQ, in, q->fdf, st));
-    return launch_calq64x(q->p, q->B2, q->fdf, q->partial, out, st);
+    return launch_calq64x(q->p, q->B2, q->fdf, q->partial, out, st, q->c64x_minb);
   }
   return launch_calq64(q->p, q->B64, in, q->partial, out, st);
 }

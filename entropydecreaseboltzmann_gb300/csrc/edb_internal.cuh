@@ -74,13 +74,15 @@ edb_status launch_calq64_reduce(const QParams &p, int nchunk, const double2 *d_p
                                 double2 *d_Q, cudaStream_t st);
 
 // FP64-accurate calQ on the FP32 pipe (double-float arithmetic): B2 is the
-// table split into (hi, lo) floats, fdf the input split into
-// {re_hi, im_hi, re_lo, im_lo}.  d_partial holds calq64x_nchunk(p) * KC.
+// table split into (hi, lo) floats, fdf (4 * N^3 float4) the input split into
+// {re_hi, im_hi, re_lo, im_lo} followed by its f_l broadcast pairs.
+// d_partial holds calq64x_nchunk(p) * KC.
 int calq64x_nchunk(const QParams &p, int *J2T_out);
 edb_status launch_split_f(long long n, const double2 *f, float4 *out, cudaStream_t st);
 edb_status launch_split_B(long long n, const double *B, float2 *B2, cudaStream_t st);
+// minb selects the register cap (2: 128 registers, 1: up to 255).
 edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const float4 *d_fdf,
-                          double2 *d_partial, double2 *d_Q, cudaStream_t st);
+                          double2 *d_partial, double2 *d_Q, cudaStream_t st, int minb);
 
 // Batched FP32 calQ (ALIASED): S solves, B32 in FFTW order.
 // variant in [0, calq32_variants()) selects the CTA-size bound (see the kernel).

@@ -24,12 +24,22 @@
 // with every operation a packed f32x2 instruction over (re, im) lanes; at the
 // end Q = (A.re - B.im, A.im + B.re), combined in FP64.
 //
-// Tiling: CTA = (output plane j1, a tile of j2, all j3) x (a chunk of row
-// planes i1).  Thread = (j2, run of 4 consecutive j3).  For each i1 the f-hat
+// Tiling: CTA = (output plane j1, a tile of j2, all j3) x (a chunk of l-lines
+// (i1, i2)).  Thread = (j2, run of 4 consecutive j3).  For each i1 the f-hat
 // m1-plane (m1 = j1 - i1 + sM mod N) is staged in shared memory; along i3 the
-// needed f_m slide down by one (a ring of 4).  B rows are streamed from HBM
-// with 16-byte loads, two rows ahead in registers.  Each CTA writes FP64
-// partial sums per row chunk; calq64_reduce_kernel adds the chunks in order.
+// needed f_m slide down by one (a ring of 4).  The number of line chunks is
+// set from the measured occupancy so the grid is whole waves.  Each CTA writes
+// FP64 partial sums per chunk; calq64_reduce_kernel adds the chunks in order.
+//
+// B stream: when every warp's row segment is a contiguous, 16-byte aligned run
+// (P % 4 == 0 and whole j2 tiles), each warp streams its own 1 KB segment of
+// the next D rows into a private shared-memory ring with 1-D TMA bulk copies
+// (lane 0 issues; one mbarrier per slot; waits bounded by %globaltimer, a
+// timeout sets the device status word).  Otherwise threads load their 32
+// bytes per row with __ldg, one row ahead.
+#include <map>
+#include <mutex>
+
 #include "edb_internal.cuh"
 
 namespace edb {
@@ -88,8 +98,61 @@ __device__ __forceinline__ void df_axpy(DF2 &acc, u64 sh2, u64 nsh2, u64 nsl2, u
   acc.h = s;
   acc.l = add2(acc.l, add2(e, pl));
 }
+
+constexpr int DEPTH = 8;  // B rows in flight per warp
+constexpr unsigned long long WAIT_LIMIT_NS = 200000000ull;
+
+__device__ __forceinline__ uint32_t s_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(s_addr(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(s_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(s_addr(dst)),
+      "l"(src), "r"(bytes), "r"(s_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(s_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long gtimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, bool &to) {
+  if (to) return;
+  if (mbar_try_wait(bar, parity)) return;
+  const unsigned long long t0 = gtimer_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (gtimer_ns() - t0 > WAIT_LIMIT_NS) {
+      to = true;
+      return;
+    }
+  }
+}
+
+__device__ int g_calq64x_status;  // nonzero: a bounded wait ran out
 }  // namespace
 
+// Splits f-hat into {re_hi, im_hi, re_lo, im_lo}.
 __global__ void fdf_split_kernel(long long n, const double2 *__restrict__ f, float4 *__restrict__ out) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -107,14 +170,30 @@ __global__ void b2_split_kernel(long long n, const double *__restrict__ B, float
   B2[i] = make_float2(h, (float)(v - (double)h));
 }
 
-template <int MAXT>
-__global__ void __launch_bounds__(MAXT, 2)
-    calq64x_kernel(QParams p, int J2T, int L1C, const float2 *__restrict__ B2,
+// TMA: per-warp bulk-copy ring for B (requires contiguous, aligned warp
+// segments; see the launcher).  Otherwise __ldg one row ahead.
+// MINB: minimum resident CTAs per SM the register allocation must allow
+// (2: at most 128 registers per thread; 1: up to 255).  Chosen per shape by
+// timing both (edb_qcalc_genB runs the comparison once per table).
+template <bool TMA, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+    calq64x_kernel(QParams p, int J2T, int LC, const float2 *__restrict__ B2,
                    const float4 *__restrict__ fdf, double2 *__restrict__ partial) {
-  extern __shared__ __align__(16) float4 plane[];  // [N][N] of the current m1
+  extern __shared__ __align__(128) unsigned char smem64[];
   const int N = p.N, P = p.P;
   const int R4 = (P + RUN - 1) / RUN;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
+  const int wthreads = min(32, (int)blockDim.x - warp * 32);  // threads in this warp
+  const long long NN = (long long)N * N;
+  // shared memory: [nwarps][DEPTH] mbarriers, B rings [nwarps][DEPTH][32 threads x 4 pairs],
+  // then the f-hat plane [N][N]
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem64);
+  float2 *rings = reinterpret_cast<float2 *>(smem64 + 16 * ((nwarps * DEPTH * 8 + 15) / 16));
+  float4 *plane = reinterpret_cast<float4 *>(rings + (TMA ? (size_t)nwarps * DEPTH * 32 * RUN : 0));
+  uint64_t *mybar = bars + warp * DEPTH;
+  float2 *myring = rings + (size_t)warp * DEPTH * 32 * RUN;
+
   const int r = tid % R4;
   const int j2l = tid / R4;
   const int j1 = blockIdx.x;
@@ -123,14 +202,37 @@ __global__ void __launch_bounds__(MAXT, 2)
   const int j2c = ok ? j2 : 0;
   const int j3_0 = r * RUN;
   const int chunk = blockIdx.z;
-  const int i1_0 = chunk * L1C, i1_1 = min(N, i1_0 + L1C);
-  const long long NN = (long long)N * N;
+  const int NL = N * N;
+  const int c0 = chunk * LC, c1 = min(NL, c0 + LC);
   const long long kcol = ((long long)j1 * P + j2c) * P + j3_0;
   // columns past P (ragged last run) read a clamped, in-row column and are
   // masked out of the output
   int colc[RUN];
 #pragma unroll
   for (int a = 0; a < RUN; ++a) colc[a] = (j3_0 + a < P) ? a : 0;
+
+  // the warp's B segment: threads [32 warp, 32 warp + wthreads) are consecutive
+  // 4-pair runs, contiguous in the row (checked by the launcher)
+  const long long wcol = ((long long)j1 * P + (blockIdx.y * J2T + (warp * 32) / R4)) * P +
+                         ((warp * 32) % R4) * RUN;
+  const uint32_t seg_bytes = (uint32_t)(wthreads * RUN * sizeof(float2));
+  const int nrows = (c1 - c0) * N;  // rows this CTA streams
+  bool to = false;
+
+  if (TMA) {
+    if (lane == 0) {
+      for (int d = 0; d < DEPTH; ++d) mbar_init(&mybar[d], 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    if (lane == 0) {  // prologue: the first DEPTH rows
+      for (int q = 0; q < DEPTH && q < nrows; ++q) {
+        const long long lflat = (long long)c0 * N + q;  // rows of the chunk are consecutive
+        mbar_expect_tx(&mybar[q], seg_bytes);
+        bulk_g2s(myring + (size_t)q * 32 * RUN, B2 + lflat * p.KC + wcol, seg_bytes, &mybar[q]);
+      }
+    }
+  }
 
   DF2 accA[RUN], accB[RUN];
 #pragma unroll
@@ -139,70 +241,121 @@ __global__ void __launch_bounds__(MAXT, 2)
     accB[a].h = accB[a].l = 0ull;
   }
 
-  for (int i1 = i1_0; i1 < i1_1; ++i1) {
-    const int m1 = ((j1 - i1 + p.sM) % N + N) % N;
-    __syncthreads();
-    for (long long e = tid; e < NN; e += blockDim.x) plane[e] = fdf[(long long)m1 * NN + e];
-    __syncthreads();
-    const int a1 = (i1 + p.sL) % N;
-    for (int i2 = 0; i2 < N; ++i2) {
-      const int m2 = ((j2c - i2 + p.sM) % N + N) % N;
-      const int a2 = (i2 + p.sL) % N;
-      const float4 *prow = plane + (long long)m2 * N;
-      const float4 *flrow = fdf + ((long long)a1 * N + a2) * N;
-      const long long lrow0 = ((long long)i1 * N + i2) * N;
-      // ring of f_m along i3: slot(a, i3) = (a - i3) mod 4
-      u64 rh[RUN], rl[RUN];
+  const int base3 = (j3_0 + p.sM) % N;  // m3 of output a = 0 at i3 = 0
+  const int fi0 = p.sL % N;             // f_l entry at i3 = 0
+  int cur_i1 = -1;
+  int q = 0;  // row counter within the chunk
+  // running line indices: i1, i2 of the line; a1, a2 = (i + sL) mod N;
+  // m2 = (j2 - i2 + sM) mod N
+  int i1 = c0 / N, i2 = c0 % N;
+  int a1 = (i1 + p.sL) % N, a2 = (i2 + p.sL) % N;
+  int m2 = ((j2c - i2 + p.sM) % N + N) % N;
+  for (int line = c0; line < c1; ++line) {
+    if (i1 != cur_i1) {  // stage the m1-plane
+      cur_i1 = i1;
+      const int m1 = ((j1 - i1 + p.sM) % N + N) % N;
+      __syncthreads();
+      for (long long e = tid; e < NN; e += blockDim.x) plane[e] = fdf[(long long)m1 * NN + e];
+      __syncthreads();
+    }
+    const float4 *prow = plane + (long long)m2 * N;
+    const float4 *flrow = fdf + ((long long)a1 * N + a2) * N;
+    const long long lrow0 = (long long)line * N;
+    u64 rh[RUN], rl[RUN];  // f_m hi, lo (re, im lanes)
 #pragma unroll
-      for (int a = 0; a < RUN; ++a) {
-        const int m3 = (j3_0 + a + p.sM) % N;
-        const float4 v = prow[m3];
-        rh[a] = pk(v.x, v.y);
-        rl[a] = pk(v.z, v.w);
-      }
-      // B rows: two in flight
-      const float2 *brow = B2 + lrow0 * p.KC + kcol;
-      float2 bcur[RUN], bnext[RUN];
+    for (int a = 0; a < RUN; ++a) {
+      int m3 = base3 + a;
+      while (m3 >= N) m3 -= N;
+      const float4 v = prow[m3];
+      rh[a] = pk(v.x, v.y);
+      rl[a] = pk(v.z, v.w);
+    }
+    const float2 *brow = B2 + lrow0 * p.KC + kcol;
+    float2 bcur[RUN], bnext[RUN];
+    // running indices along i3: the new ring entry m3 = (j3_0 - i3 + sM) mod N
+    // and the f_l entry fi = (i3 + sL) mod N, kept in range by one conditional
+    int m3n = base3;  // value at i3 = 0
+    int fi = fi0;
+    if (!TMA) {
 #pragma unroll
       for (int a = 0; a < RUN; ++a) bcur[a] = __ldg(brow + colc[a]);
-      for (int g = 0; g < N; g += RUN) {
+    }
+    for (int g = 0; g < N; g += RUN) {
 #pragma unroll
-        for (int t = 0; t < RUN; ++t) {
-          const int i3 = g + t;
-          if (i3 >= N) break;
-          if (i3 + 1 < N) {
-            const float2 *bn = brow + (long long)(i3 + 1) * p.KC;
+      for (int t = 0; t < RUN; ++t, ++q) {
+        const int i3 = g + t;
+        if (i3 >= N) break;
+        if (TMA) {
+          const int slot = q % DEPTH;
+          mbar_wait(&mybar[slot], (uint32_t)((q / DEPTH) & 1), to);
+          const float4 *src = reinterpret_cast<const float4 *>(myring + ((size_t)slot * 32 + lane) * RUN);
+          const float4 v0 = src[0], v1 = src[1];
+          bcur[0] = make_float2(v0.x, v0.y);
+          bcur[1] = make_float2(v0.z, v0.w);
+          bcur[2] = make_float2(v1.x, v1.y);
+          bcur[3] = make_float2(v1.z, v1.w);
+          __syncwarp();
+          if (lane == 0 && q + DEPTH < nrows) {  // refill this slot with row q + DEPTH
+            const long long lflat = (long long)c0 * N + q + DEPTH;
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(&mybar[slot], seg_bytes);
+            bulk_g2s(myring + (size_t)slot * 32 * RUN, B2 + lflat * p.KC + wcol, seg_bytes,
+                     &mybar[slot]);
+          }
+        } else if (i3 + 1 < N) {
+          const float2 *bn = brow + (long long)(i3 + 1) * p.KC;
 #pragma unroll
-            for (int a = 0; a < RUN; ++a) bnext[a] = __ldg(bn + colc[a]);
-          }
-          if (i3 > 0) {  // new ring value enters at a = 0
-            int m3 = (j3_0 - i3 + p.sM) % N;
-            if (m3 < 0) m3 += N;
-            const float4 v = prow[m3];
-            const int slot = (RUN - t) % RUN;
-            rh[slot] = pk(v.x, v.y);
-            rl[slot] = pk(v.z, v.w);
-          }
-          const float4 fl = __ldg(flrow + (i3 + p.sL) % N);
-          // broadcast pairs of f_l.re and f_l.im (hi; and negated hi, lo)
-          const u64 xr = pk(fl.x, fl.x), nxr = pk(-fl.x, -fl.x), nlr = pk(-fl.z, -fl.z);
-          const u64 xi = pk(fl.y, fl.y), nxi = pk(-fl.y, -fl.y), nli = pk(-fl.w, -fl.w);
+          for (int a = 0; a < RUN; ++a) bnext[a] = __ldg(bn + colc[a]);
+        }
+        if (i3 > 0) {  // new ring value enters at a = 0
+          m3n = (m3n == 0) ? N - 1 : m3n - 1;
+          const float4 v = prow[m3n];
+          const int slot = (RUN - t) % RUN;
+          rh[slot] = pk(v.x, v.y);
+          rl[slot] = pk(v.z, v.w);
+        }
+        // broadcast pairs of f_l.re and f_l.im (hi; and negated hi, lo)
+        const float4 fl = __ldg(flrow + fi);
+        fi = (fi + 1 == N) ? 0 : fi + 1;
+        const u64 xr = pk(fl.x, fl.x), nxr = pk(-fl.x, -fl.x), nlr = pk(-fl.z, -fl.z);
+        const u64 xi = pk(fl.y, fl.y), nxi = pk(-fl.y, -fl.y), nli = pk(-fl.w, -fl.w);
 #pragma unroll
-          for (int a = 0; a < RUN; ++a) {
-            const int slot = (a - t + RUN) % RUN;
-            const float bh = bcur[a].x, bl = bcur[a].y;
-            const u64 nbh2 = pk(-bh, -bh), bh2 = pk(bh, bh), bl2 = pk(bl, bl);
-            // u = b * f_m:  nu_h = -(b_h f_m,h), uc = exact error + cross terms
-            const u64 nu_h = mul2(nbh2, rh[slot]);
-            const u64 ue = fma2(bh2, rh[slot], nu_h);
-            const u64 uc = fma2(bh2, rl[slot], fma2(bl2, rh[slot], ue));
-            df_axpy(accA[a], xr, nxr, nlr, nu_h, uc);
-            df_axpy(accB[a], xi, nxi, nli, nu_h, uc);
-          }
+        for (int a = 0; a < RUN; ++a) {
+          const int slot = (a - t + RUN) % RUN;
+          const float bh = bcur[a].x, bl = bcur[a].y;
+          const u64 nbh2 = pk(-bh, -bh), bh2 = pk(bh, bh), bl2 = pk(bl, bl);
+          // u = b * f_m:  nu_h = -(b_h f_m,h), uc = exact error + cross terms
+          const u64 nu_h = mul2(nbh2, rh[slot]);
+          const u64 ue = fma2(bh2, rh[slot], nu_h);
+          const u64 uc = fma2(bh2, rl[slot], fma2(bl2, rh[slot], ue));
+          df_axpy(accA[a], xr, nxr, nlr, nu_h, uc);
+          df_axpy(accB[a], xi, nxi, nli, nu_h, uc);
+        }
+        if (!TMA) {
 #pragma unroll
           for (int a = 0; a < RUN; ++a) bcur[a] = bnext[a];
         }
       }
+    }
+    // next line
+    if (++i2 == N) {
+      i2 = 0;
+      ++i1;
+      a1 = (a1 + 1 == N) ? 0 : a1 + 1;
+    }
+    a2 = (a2 + 1 == N) ? 0 : a2 + 1;
+    m2 = (m2 == 0) ? N - 1 : m2 - 1;
+  }
+  if (TMA) {
+    if (__syncthreads_or(to)) {
+      if (lane == 0) {
+        atomicExch(&g_calq64x_status, 1);
+        bool t2 = false;  // drain the slots still in flight
+        for (int qq = (nrows > DEPTH ? nrows - DEPTH : 0); qq < nrows; ++qq)
+          mbar_wait(&mybar[qq % DEPTH], (uint32_t)((qq / DEPTH) & 1), t2);
+      }
+      __syncwarp();
+      return;
     }
   }
   if (!ok) return;
@@ -217,19 +370,98 @@ __global__ void __launch_bounds__(MAXT, 2)
   }
 }
 
-// Chunks over i1 so that the grid covers the SMs a few times over.
-int calq64x_nchunk(const QParams &p, int *J2T_out) {
+struct C64xPlan {
+  int J2T, tiles, threads, LC, nch;
+  bool tma;
+  size_t smem;
+};
+
+template <bool TMA>
+static const void *c64x_fn(int minb) {
+  return minb == 2 ? (const void *)calq64x_kernel<TMA, 2> : (const void *)calq64x_kernel<TMA, 1>;
+}
+
+static size_t c64x_smem(int N, int threads, bool tma) {
+  const int nwarps = (threads + 31) / 32;
+  size_t o = 16 * (size_t)((nwarps * DEPTH * 8 + 15) / 16);
+  if (tma) o += sizeof(float2) * (size_t)nwarps * DEPTH * 32 * RUN;
+  return o + sizeof(float4) * (size_t)N * N;
+}
+
+// Tile shape, TMA eligibility and the line-chunk count that makes the grid
+// whole waves of resident CTAs (cached per shape: the occupancy query is not
+// free).
+static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int minb);
+static C64xPlan c64x_plan(const QParams &p, bool aligned, int minb) {
+  static std::mutex mu;
+  static std::map<long long, C64xPlan> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const long long key =
+      ((((long long)dev * 128 + p.N) * 4 + p.mode) * 2 + (aligned ? 1 : 0)) * 4 + minb;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  C64xPlan pl = c64x_plan_compute(p, aligned, minb);
+  cache[key] = pl;
+  return pl;
+}
+
+static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int minb) {
+  C64xPlan pl;
   const int R4 = (p.P + RUN - 1) / RUN;
   int J2T = 256 / R4;
   if (J2T > p.P) J2T = p.P;
   const int tiles = (p.P + J2T - 1) / J2T;
   J2T = (p.P + tiles - 1) / tiles;
-  if (J2T_out) *J2T_out = J2T;
-  long long ctas = (long long)p.P * tiles;
-  int nchunk = (int)((4LL * 152 + ctas - 1) / ctas);
-  if (nchunk > p.N) nchunk = p.N;
-  if (nchunk < 1) nchunk = 1;
-  return nchunk;
+  pl.J2T = J2T;
+  pl.tiles = tiles;
+  pl.threads = J2T * R4;
+  pl.tma = aligned && (p.P % RUN) == 0 && (p.P % J2T) == 0;
+  pl.smem = c64x_smem(p.N, pl.threads, pl.tma);
+  int occ = 1;
+  const void *fn = pl.tma ? c64x_fn<true>(minb) : c64x_fn<false>(minb);
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, pl.threads, pl.smem);
+  if (occ < 1) occ = 1;
+  int sms = 152, dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long wave = (long long)sms * occ;
+  const long long per_chunk = (long long)p.P * tiles;
+  const int NL = p.N * p.N;
+  // chunk count that best fills whole waves (at most 8) with balanced chunks:
+  // efficiency = useful CTA-lines / (waves * wave * lines per chunk)
+  double best_eff = -1.0;
+  int best_lc = NL;
+  for (int ch = 1; ch <= NL; ++ch) {
+    const int lc = (NL + ch - 1) / ch;
+    const int nch = (NL + lc - 1) / lc;
+    if (nch != ch) continue;
+    const long long ctas = per_chunk * nch;
+    const long long waves = (ctas + wave - 1) / wave;
+    if (waves > 8) break;
+    const double eff = (double)per_chunk * NL / ((double)waves * wave * lc);
+    if (eff > best_eff + 1e-9) {
+      best_eff = eff;
+      best_lc = lc;
+    }
+  }
+  pl.LC = best_lc;
+  pl.nch = (NL + best_lc - 1) / best_lc;
+  return pl;
+}
+
+int calq64x_nchunk(const QParams &p, int *J2T_out) {
+  // upper bound over the variants, used to size the partial-sum buffer
+  int n = 1;
+  for (int minb = 1; minb <= 2; ++minb)
+    for (int al = 0; al <= 1; ++al) {
+      const C64xPlan pl = c64x_plan(p, al != 0, minb);
+      if (J2T_out) *J2T_out = pl.J2T;
+      if (pl.nch > n) n = pl.nch;
+    }
+  return n;
 }
 
 edb_status launch_split_f(long long n, const double2 *f, float4 *out, cudaStream_t st) {
@@ -245,26 +477,28 @@ edb_status launch_split_B(long long n, const double *B, float2 *B2, cudaStream_t
 }
 
 edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const float4 *d_fdf,
-                          double2 *d_partial, double2 *d_Q, cudaStream_t st) {
-  int J2T = 0;
-  const int nchunk = calq64x_nchunk(p, &J2T);
-  const int L1C = (p.N + nchunk - 1) / nchunk;
-  const int nch = (p.N + L1C - 1) / L1C;
-  const int R4 = (p.P + RUN - 1) / RUN;
-  const int threads = J2T * R4;
-  const int tiles = (p.P + J2T - 1) / J2T;
-  const size_t smem = sizeof(float4) * (size_t)p.N * p.N;
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(calq64x_kernel<256>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(calq64x)");
-    configured = true;
+                          double2 *d_partial, double2 *d_Q, cudaStream_t st, int minb) {
+  if (minb != 1) minb = 2;
+  const bool aligned = ((uintptr_t)d_B2 % 16) == 0;
+  const C64xPlan pl = c64x_plan(p, aligned, minb);
+  dim3 grid((unsigned)p.P, (unsigned)pl.tiles, (unsigned)pl.nch);
+  if (pl.tma) {
+    if (minb == 2)
+      calq64x_kernel<true, 2><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, d_B2, d_fdf,
+                                                                 d_partial);
+    else
+      calq64x_kernel<true, 1><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, d_B2, d_fdf,
+                                                                 d_partial);
+  } else {
+    if (minb == 2)
+      calq64x_kernel<false, 2><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, d_B2, d_fdf,
+                                                                  d_partial);
+    else
+      calq64x_kernel<false, 1><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, d_B2, d_fdf,
+                                                                  d_partial);
   }
-  dim3 grid((unsigned)p.P, (unsigned)tiles, (unsigned)nch);
-  calq64x_kernel<256><<<grid, threads, smem, st>>>(p, J2T, L1C, d_B2, d_fdf, d_partial);
   EDB_LAUNCHED();
-  return launch_calq64_reduce(p, nch, d_partial, d_Q, st);
+  return launch_calq64_reduce(p, pl.nch, d_partial, d_Q, st);
 }
 
 }  // namespace edb
