@@ -43,12 +43,12 @@ class QCalcInfo(C.Structure):
 
 class SolverDesc(C.Structure):
     _fields_ = [("N", C.c_int), ("R", C.c_double), ("scheme", C.c_int), ("fix_entropy", C.c_int),
-                ("beta", C.c_double), ("kernel", QCalcDesc)]
+                ("beta", C.c_double), ("kernel", QCalcDesc), ("conserve", C.c_int)]
 
 
 class BatchDesc(C.Structure):
     _fields_ = [("S", C.c_int), ("N", C.c_int), ("R", C.c_double), ("scheme", C.c_int),
-                ("dt", C.c_double), ("fix_entropy", C.c_int)]
+                ("dt", C.c_double), ("fix_entropy", C.c_int), ("conserve", C.c_int)]
 
 
 _dp = C.POINTER(C.c_double)
@@ -107,6 +107,10 @@ def _load():
         "edb_batch_read": (C.c_int, [_vp, _dp, _dp]),
         "edb_batch_moments": (C.c_int, [_vp, _dp, _dp]),
         "edb_batch_launches_per_step": (C.c_int, [_vp, _ip]),
+        "edb_moments_hat_device": (C.c_int, [C.c_int, C.c_int, C.c_double, _vp, _vp, _vp]),
+        "edb_moments_project_device": (C.c_int, [C.c_int, C.c_int, C.c_double, _vp, _vp, _vp]),
+        "edb_maxwellian_fit_device": (C.c_int, [C.c_int, C.c_int, C.c_double, _vp, _vp, _vp,
+                                                _vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

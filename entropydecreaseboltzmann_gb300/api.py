@@ -227,8 +227,11 @@ class BKW3D:
     """
 
     def __init__(self, N0: int, R: float, *, gamma: float = 0.0, L: float = R_REFERENCE,
-                 filter: bool = True, index_mode: int = INDEX_REFERENCE):
+                 filter: bool = True, index_mode: int = INDEX_REFERENCE, conserve: bool = False):
         self.N0 = int(N0)
+        # conservative mode (no reference counterpart): moments projected back
+        # after every step, moment-preserving entropy fix fed back into Fhat
+        self.conserve = bool(conserve)
         self.R = float(R)
         self.N3d = self.N0 ** 3
         self.kernel = dict(gamma=float(gamma), L=float(L), filter=bool(filter),
@@ -260,6 +263,7 @@ class BKW3D:
         d.kernel.L = self.kernel["L"]
         d.kernel.filter = int(self.kernel["filter"])
         d.kernel.index_mode = self.kernel["index_mode"]
+        d.conserve = int(self.conserve)
         h = C.c_void_p()
         check(lib.edb_solver_create(C.byref(d), C.byref(h)))
         try:
@@ -309,8 +313,9 @@ class BatchSolver:
     """
 
     def __init__(self, qcalc: QCalculator, S: int, R: float, scheme: int = SCHEME_RK4,
-                 dt: float = 0.01, fix_entropy: bool = False):
+                 dt: float = 0.01, fix_entropy: bool = False, conserve: bool = False):
         d = BatchDesc()
+        d.conserve = int(bool(conserve))
         d.S = int(S)
         d.N = qcalc.N
         d.R = float(R)
@@ -367,3 +372,29 @@ class BatchSolver:
                 self._h = None
         except Exception:
             pass
+
+
+# ------------------------------------------------------------ conservation
+# No reference counterpart: the moment functionals of conservative mode.  The
+# arrays are torch CUDA tensors (complex128, S x N^3, FFTW order) or device
+# addresses.
+
+def moments_hat(N: int, R: float, Fhat, out, S: int = 1, stream=None):
+    """Grid moments h^3 sum Re F {1, v1, v2, v3, |v|^2} of S solves from Fhat
+    into `out` (S x 5 float64 on the device)."""
+    check(lib.edb_moments_hat_device(int(N), int(S), float(R), devptr(Fhat), devptr(out),
+                                     stream_ptr(stream)))
+
+
+def moments_project(N: int, R: float, Fhat, m0, S: int = 1, stream=None):
+    """Minimum-norm correction of Fhat (in place) onto the moments m0 (S x 5)."""
+    check(lib.edb_moments_project_device(int(N), int(S), float(R), devptr(Fhat), devptr(m0),
+                                         stream_ptr(stream)))
+
+
+def maxwellian_fit(N: int, R: float, F, theta, status, S: int = 1, stream=None):
+    """Discrete Maxwellian of Re F per solve, written into Im F; theta (S x 5
+    float64) = (a, b1, b2, b3, c) of exp(a + b.v + c|v|^2); status (S int32) =
+    Newton iterations or -1."""
+    check(lib.edb_maxwellian_fit_device(int(N), int(S), float(R), devptr(F), devptr(theta),
+                                        devptr(status), stream_ptr(stream)))

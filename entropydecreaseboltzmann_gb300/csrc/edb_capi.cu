@@ -36,25 +36,6 @@ edb_status ensure_device() {
   return EDB_OK;
 }
 
-template <typename T>
-static edb_status dalloc(T **p, size_t count) {
-  *p = nullptr;
-  if (count == 0) return EDB_OK;
-  cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
-  if (e != cudaSuccess) {
-    *p = nullptr;
-    cudaGetLastError();
-    return fail(EDB_ENOMEM, std::string("cudaMalloc of ") + std::to_string(count * sizeof(T)) +
-                                " bytes failed: " + cudaGetErrorString(e));
-  }
-  return EDB_OK;
-}
-template <typename T>
-static void dfree(T *&p) {
-  if (p) cudaFree((void *)p);
-  p = nullptr;
-}
-
 }  // namespace edb
 
 using namespace edb;
@@ -79,6 +60,15 @@ extern "C" const char *edb_status_string(edb_status s) {
 
 extern "C" int edb_version(void) { return 100; }
 extern "C" long long edb_kernel_launch_count(void) { return g_launches.load(); }
+
+// Uploads the conservation table of (N, R) (see edb_kernels_conserve.cu).
+static edb_status upload_conserve_table(int N, double R, double **d_tab) {
+  std::vector<double> tab;
+  build_conserve_table(N, R, tab);
+  if (!*d_tab) EDB_TRY(dalloc(d_tab, tab.size()));
+  EDB_CUDA(cudaMemcpy(*d_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
+  return EDB_OK;
+}
 
 // =============================================================== QCalculator
 
@@ -534,6 +524,9 @@ struct edb_solver {
   int trace_cap = 0, trace_n = 0;
   bool has_initial = false;
   std::vector<double> F0;
+  // conservative mode: moment table, initial moments, forward-DFT scratch
+  double *ctab = nullptr, *m0 = nullptr;
+  double2 *tmp = nullptr;
 };
 
 extern "C" edb_status edb_solver_create(const edb_solver_desc *d, edb_solver **out) {
@@ -559,6 +552,11 @@ extern "C" edb_status edb_solver_create(const edb_solver_desc *d, edb_solver **o
   for (int i = 0; i < 4 && rc == EDB_OK; ++i) rc = dalloc(&s->Qs[i], NQ);
   for (int i = 0; i < 3 && rc == EDB_OK; ++i) rc = dalloc(&s->Fs[i], NQ);
   if (rc == EDB_OK) rc = dalloc(&s->state, 1);
+  if (rc == EDB_OK && d->conserve) {
+    rc = upload_conserve_table(d->N, d->R, &s->ctab);
+    if (rc == EDB_OK) rc = dalloc(&s->m0, 5);
+    if (rc == EDB_OK) rc = dalloc(&s->tmp, NQ);
+  }
   if (rc != EDB_OK) {
     edb_solver_destroy(s);
     return rc;
@@ -578,6 +576,9 @@ extern "C" edb_status edb_solver_destroy(edb_solver *s) {
   dfree(s->state);
   dfree(s->tr_raw);
   dfree(s->tr_fixed);
+  dfree(s->ctab);
+  dfree(s->m0);
+  dfree(s->tmp);
   if (s->q) edb_qcalc_destroy(s->q);
   if (s->st) cudaStreamDestroy(s->st);
   delete s;
@@ -673,14 +674,24 @@ static edb_status solver_step(edb_solver *s, double dt, bool dufort_startup) {
       }
       break;
   }
+  // conservative mode: back onto the initial moments
+  if (s->d.conserve) EDB_TRY(launch_project_moments(s->d.N, 1, s->ctab, Fh, s->m0, st));
   // fft3(isInverse) then calEntropy and the fix rule
   EDB_TRY(launch_dft3d(s->d.N, 1, Fh, s->F, nullptr, 1, 0, st));
   int fix_mode = 0;
   if (s->d.scheme == EDB_SCHEME_FE) fix_mode = s->d.fix_entropy ? 1 : 0;
   else if (s->d.scheme == EDB_SCHEME_CFE) fix_mode = s->d.fix_entropy ? 2 : 0;
   else if (s->d.scheme == EDB_SCHEME_SSP3 || s->d.scheme == EDB_SCHEME_RK4) fix_mode = 2;
-  EDB_TRY(launch_step_entropy(s->d.N, 1, s->d.R, s->F, s->state, 1.0e-10, fix_mode, s->tr_raw,
-                              s->tr_fixed, s->trace_cap, st));
+  if (s->d.conserve) {
+    // moment-preserving fix, fed back into Fhat
+    EDB_TRY(launch_step_entropy_conserve(s->d.N, 1, s->d.R, s->F, s->state, 1.0e-10, fix_mode,
+                                         s->tr_raw, s->tr_fixed, s->trace_cap, st));
+    EDB_TRY(launch_dft3d(s->d.N, 1, s->F, s->tmp, nullptr, 0, 0, st));
+    EDB_TRY(launch_masked_copy(n, 1, s->state, s->tmp, Fh, st));
+  } else {
+    EDB_TRY(launch_step_entropy(s->d.N, 1, s->d.R, s->F, s->state, 1.0e-10, fix_mode, s->tr_raw,
+                                s->tr_fixed, s->trace_cap, st));
+  }
   if (s->d.scheme == EDB_SCHEME_DUFORT && !dufort_startup)
     EDB_CUDA(cudaMemcpyAsync(s->Fold, F[0], sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
   return EDB_OK;
@@ -704,13 +715,16 @@ extern "C" edb_status edb_solver_run(edb_solver *s, double T0, double TEnd, doub
   else
     EDB_TRY(launch_sinusoid_init(s->d.N, s->d.R, s->F, st));
   EDB_TRY(launch_dft3d(s->d.N, 1, s->F, s->Fhat, nullptr, 0, 0, st));
+  if (s->d.conserve) EDB_TRY(launch_hat_moments(s->d.N, 1, s->ctab, s->Fhat, s->m0, st));
   if (s->d.scheme == EDB_SCHEME_DUFORT)
     EDB_CUDA(cudaMemcpyAsync(s->Fold, s->Fhat, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
   // entropy0 and the step counter: FE starts from calEntropy() and step 1
   // (BKW.h:214-216); the others from 1. and step 0.
   EfixState init = {1.0, 0, 0, 1.0, 0, 0};
   EDB_CUDA(cudaMemcpyAsync(s->state, &init, sizeof(init), cudaMemcpyHostToDevice, st));
-  if (s->d.scheme == EDB_SCHEME_FE) {
+  // conservative mode also starts from the initial entropy, so the fix can
+  // act from the first step
+  if (s->d.scheme == EDB_SCHEME_FE || s->d.conserve) {
     EDB_TRY(launch_calentropy(s->d.N, 1, s->d.R, s->F, &s->state->H_prev, st));
     int one = 1;
     EDB_CUDA(cudaMemcpyAsync(&s->state->step, &one, sizeof(int), cudaMemcpyHostToDevice, st));
@@ -785,6 +799,7 @@ struct edb_batch {
   EfixState *state = nullptr;
   double *tr_raw = nullptr, *tr_fixed = nullptr;
   double *mom = nullptr, *H = nullptr;
+  double *ctab = nullptr, *m0 = nullptr;  // conservative mode
   cudaGraphExec_t exec = nullptr;
   cudaStream_t exec_stream = nullptr;
   int launches_per_step = 0;
@@ -820,6 +835,12 @@ extern "C" edb_status edb_batch_create(edb_qcalc *q, const edb_batch_desc *d, ed
   if (rc == EDB_OK) rc = dalloc(&b->H, (size_t)d->S);
   if (rc == EDB_OK) rc = dalloc(&b->tr_raw, (size_t)d->S);
   if (rc == EDB_OK) rc = dalloc(&b->tr_fixed, (size_t)d->S);
+  if (rc == EDB_OK && d->conserve) {
+    rc = upload_conserve_table(d->N, d->R, &b->ctab);
+    if (rc == EDB_OK) rc = dalloc(&b->m0, (size_t)d->S * 5);
+    // the forward transform of a fixed F needs a scratch array
+    if (rc == EDB_OK && nstage == 0) rc = dalloc(&b->Fs[0], n);
+  }
   if (rc != EDB_OK) {
     edb_batch_destroy(b);
     return rc;
@@ -842,6 +863,8 @@ extern "C" edb_status edb_batch_destroy(edb_batch *b) {
   dfree(b->H);
   dfree(b->tr_raw);
   dfree(b->tr_fixed);
+  dfree(b->ctab);
+  dfree(b->m0);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
   return EDB_OK;
@@ -850,6 +873,7 @@ extern "C" edb_status edb_batch_destroy(edb_batch *b) {
 static edb_status batch_init_state(edb_batch *b, cudaStream_t st) {
   // Fhat = fft(F) in FP64, its FP32 copy, entropy bookkeeping reset
   EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->F, b->Fhat, nullptr, 0, 0, st));
+  if (b->d.conserve) EDB_TRY(launch_hat_moments(b->d.N, b->d.S, b->ctab, b->Fhat, b->m0, st));
   EDB_TRY(launch_d2f(b->n, b->Fhat, b->in32, st));
   // pick the batched kernel's variant for this S on real data, before the
   // step graph is captured (the graph bakes the choice in)
@@ -859,6 +883,10 @@ static edb_status batch_init_state(edb_batch *b, cudaStream_t st) {
   std::vector<EfixState> init((size_t)b->d.S, EfixState{1.0, 0, 0, 1.0, 0, 0});
   EDB_CUDA(cudaMemcpyAsync(b->state, init.data(), sizeof(EfixState) * b->d.S,
                            cudaMemcpyHostToDevice, st));
+  if (b->d.conserve) {  // start the entropy rule from the initial entropy
+    EDB_TRY(launch_calentropy(b->d.N, b->d.S, b->d.R, b->F, b->H, st));
+    EDB_TRY(launch_state_from_entropy(b->d.S, b->H, b->state, st));
+  }
   EDB_CUDA(cudaStreamSynchronize(st));
   return EDB_OK;
 }
@@ -924,7 +952,19 @@ static edb_status batch_step_record(edb_batch *b, cudaStream_t st) {
                                 in, st));
       break;
   }
-  if (b->d.fix_entropy) {
+  if (b->d.conserve) {
+    // back onto the initial moments; the fix (moment-preserving) feeds the
+    // fixed F back into Fhat; the FP32 copy follows the final Fhat
+    EDB_TRY(launch_project_moments(N, S, b->ctab, Fh, b->m0, st));
+    if (b->d.fix_entropy) {
+      EDB_TRY(launch_dft3d(N, S, Fh, b->F, nullptr, 1, 0, st));
+      EDB_TRY(launch_step_entropy_conserve(N, S, b->d.R, b->F, b->state, 1.0e-10, 2, b->tr_raw,
+                                           b->tr_fixed, 1, st));
+      EDB_TRY(launch_dft3d(N, S, b->F, F[0], nullptr, 0, 0, st));
+      EDB_TRY(launch_masked_copy(b->NQ, S, b->state, F[0], Fh, st));
+    }
+    EDB_TRY(launch_d2f(n, Fh, in, st));
+  } else if (b->d.fix_entropy) {
     EDB_TRY(launch_dft3d(N, S, Fh, b->F, nullptr, 1, 0, st));
     EDB_TRY(launch_step_entropy(N, S, b->d.R, b->F, b->state, 1.0e-10, 2, b->tr_raw, b->tr_fixed,
                                 1, st));
@@ -995,6 +1035,51 @@ extern "C" edb_status edb_batch_moments(edb_batch *b, double *moments, double *e
 extern "C" edb_status edb_batch_launches_per_step(edb_batch *b, int *n) {
   if (!b || !n) return fail(EDB_EINVAL, "null argument");
   *n = b->launches_per_step;
+  return EDB_OK;
+}
+
+// ============================================================ conservation
+
+extern "C" edb_status edb_moments_hat_device(int N, int S, double R, const double *d_Fhat,
+                                             double *d_m, void *stream) {
+  if (N < 3 || N > 64 || S < 1 || !(R > 0) || !d_Fhat || !d_m)
+    return fail(EDB_EINVAL, "bad argument");
+  EDB_TRY(ensure_device());
+  double *tab = nullptr;
+  EDB_TRY(upload_conserve_table(N, R, &tab));
+  cudaStream_t st = (cudaStream_t)stream;
+  edb_status rc = launch_hat_moments(N, S, tab, (const double2 *)d_Fhat, d_m, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  dfree(tab);
+  if (rc != EDB_OK) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "moments");
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_moments_project_device(int N, int S, double R, double *d_Fhat,
+                                                 const double *d_m0, void *stream) {
+  if (N < 3 || N > 64 || S < 1 || !(R > 0) || !d_Fhat || !d_m0)
+    return fail(EDB_EINVAL, "bad argument");
+  EDB_TRY(ensure_device());
+  double *tab = nullptr;
+  EDB_TRY(upload_conserve_table(N, R, &tab));
+  cudaStream_t st = (cudaStream_t)stream;
+  edb_status rc = launch_project_moments(N, S, tab, (double2 *)d_Fhat, d_m0, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  dfree(tab);
+  if (rc != EDB_OK) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "moment projection");
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_maxwellian_fit_device(int N, int S, double R, double *d_F,
+                                                double *d_theta, int *d_status, void *stream) {
+  if (N < 3 || N > 64 || S < 1 || !(R > 0) || !d_F || !d_theta || !d_status)
+    return fail(EDB_EINVAL, "bad argument");
+  EDB_TRY(ensure_device());
+  cudaStream_t st = (cudaStream_t)stream;
+  EDB_TRY(launch_maxwellian_fit(N, S, R, (double2 *)d_F, d_theta, d_status, st));
+  EDB_CUDA(cudaStreamSynchronize(st));
   return EDB_OK;
 }
 

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/edb.h"
 
@@ -37,6 +38,26 @@ void count_launch(int n = 1);
   } while (0)
 
 edb_status ensure_device();
+
+// Device allocation of `count` elements of T (EDB_ENOMEM on failure).
+template <typename T>
+inline edb_status dalloc(T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return EDB_OK;
+  cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(EDB_ENOMEM, std::string("cudaMalloc of ") + std::to_string(count * sizeof(T)) +
+                                " bytes failed: " + cudaGetErrorString(e));
+  }
+  return EDB_OK;
+}
+template <typename T>
+inline void dfree(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
 
 // ------------------------------------------------------------ parameters
 // Index parameters of one collision sum (both index modes).  With i the
@@ -74,8 +95,8 @@ edb_status launch_calq64_reduce(const QParams &p, int nchunk, const double2 *d_p
                                 double2 *d_Q, cudaStream_t st);
 
 // FP64-accurate calQ on the FP32 pipe (double-float arithmetic): B2 is the
-// table split into (hi, lo) floats, fdf (4 * N^3 float4) the input split into
-// {re_hi, im_hi, re_lo, im_lo} followed by its f_l broadcast pairs.
+// table split into (hi, lo) floats, fdf (N^3 float4) the input split into
+// {re_hi, im_hi, re_lo, im_lo}.
 // d_partial holds calq64x_nchunk(p) * KC.
 int calq64x_nchunk(const QParams &p, int *J2T_out);
 edb_status launch_split_f(long long n, const double2 *f, float4 *out, cudaStream_t st);
@@ -101,7 +122,7 @@ edb_status launch_dft3d(int N, int batch, const void *d_in, void *d_out, void *d
 struct EfixState {
   double avg;       // Averagef (EntropyFix.h:20)
   int avg_flag;     // Average_flag (EntropyFix.h:22)
-  int pad;
+  int fixed;        // conservative mode: the last step's fix changed F
   double H_prev;    // entropy0 of the integrator loop
   int step;         // integrator step counter (BKW.h:216, 278, ...)
   int rec;          // trace records written
@@ -141,5 +162,27 @@ edb_status launch_sinusoid_init(int N, double R, double2 *d_F, cudaStream_t st);
 // moments (mass, momentum, energy) of Re F per solve, FP64.
 edb_status launch_moments(int N, int batch, double R, const double2 *d_F, double *d_out,
                           cudaStream_t st);
+
+// ---- conservation (edb_kernels_conserve.cu)
+// Table per (N, R): W1, W2 (N complex each), G^-1 (25), h^3.
+inline int conserve_table_len(int N) { return 4 * N + 32; }
+void build_conserve_table(int N, double R, std::vector<double> &tab);
+// Grid moments h^3 sum F {1, v1, v2, v3, |v|^2} of S solves from F-hat.
+edb_status launch_hat_moments(int N, int S, const double *d_tab, const double2 *d_Fhat,
+                              double *d_out, cudaStream_t st);
+// Minimum-norm correction of F-hat onto the moments d_m0 (S x 5).
+edb_status launch_project_moments(int N, int S, const double *d_tab, double2 *d_Fhat,
+                                  const double *d_m0, cudaStream_t st);
+// Post-step rule with the moment-preserving fix (sets EfixState::fixed).
+edb_status launch_step_entropy_conserve(int N, int batch, double R, double2 *d_F,
+                                        EfixState *d_state, double eps, int fix_mode,
+                                        double *d_trace_raw, double *d_trace_fixed,
+                                        int trace_cap, cudaStream_t st);
+edb_status launch_maxwellian_fit(int N, int S, double R, double2 *d_F, double *d_theta,
+                                 int *d_status, cudaStream_t st);
+edb_status launch_state_from_entropy(int S, const double *d_H, EfixState *d_state,
+                                     cudaStream_t st);
+edb_status launch_masked_copy(long long NQ, int S, const EfixState *d_state,
+                              const double2 *d_src, double2 *d_dst, cudaStream_t st);
 
 }  // namespace edb

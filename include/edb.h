@@ -218,6 +218,10 @@ typedef struct {
   int fix_entropy;   /* setFixEntropy (BKW.h:46); FE and CFE consult it, SSP3/RK4 fix regardless */
   double beta;       /* CFE / DUFORT parameter */
   edb_qcalc_desc kernel; /* the reference uses QCalculator(N0, 0): gamma 0, L 6.62132, filter on */
+  int conserve;      /* 0: the reference's behaviour.  1: conservative mode (no reference
+                        counterpart): after every step Fhat is projected back onto its initial
+                        mass, momentum and energy, and the entropy fix blends toward the discrete
+                        Maxwellian of f (moment-preserving) and is fed back into Fhat */
 } edb_solver_desc;
 
 typedef struct edb_solver edb_solver;
@@ -244,6 +248,7 @@ typedef struct {
   int scheme;        /* EDB_SCHEME_FE, EDB_SCHEME_SSP3 or EDB_SCHEME_RK4 */
   double dt;
   int fix_entropy;   /* apply the EntropyFix rule after each step (FP64) */
+  int conserve;      /* conservative mode, as in edb_solver_desc */
 } edb_batch_desc;
 
 typedef struct edb_batch edb_batch;
@@ -265,6 +270,26 @@ edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat);
 edb_status edb_batch_moments(edb_batch *b, double *moments, double *entropy);
 /* Kernel launches per step of the captured graph. */
 edb_status edb_batch_launches_per_step(edb_batch *b, int *n);
+
+/* -------------------------------------------------------- conservation */
+/* No reference counterpart: the moment functionals of conservative mode.
+ * Grid moments h^3 sum_j Re F_j {1, v1, v2, v3, |v|^2} (v_j = -R + j h,
+ * h = 2R/N) of S solves, computed from Fhat (S x N^3 complex, FFTW order,
+ * device) into d_m (S x 5 doubles, device).  Synchronous. */
+edb_status edb_moments_hat_device(int N, int S, double R, const double *d_Fhat, double *d_m,
+                                  void *stream);
+/* Minimum-norm (Euclidean) correction of each solve's Fhat so that its grid
+ * moments equal d_m0 (S x 5): F <- F - C^T (C C^T)^-1 (C F - m0), applied on
+ * the three axis lines of Fhat.  Synchronous. */
+edb_status edb_moments_project_device(int N, int S, double R, double *d_Fhat, const double *d_m0,
+                                      void *stream);
+/* Discrete Maxwellian fit: for each of S solves with f = Re F (S x N^3
+ * complex, device), finds M = exp(a + b.v + c|v|^2) whose grid moments equal
+ * f's (Newton on the Lagrange multipliers), writes M into Im F, theta (S x 5:
+ * a, b1, b2, b3, c) and status (S ints: Newton iterations, or -1 when f has
+ * no positive mass/temperature or Newton failed).  Synchronous. */
+edb_status edb_maxwellian_fit_device(int N, int S, double R, double *d_F, double *d_theta,
+                                     int *d_status, void *stream);
 
 #ifdef __cplusplus
 }
