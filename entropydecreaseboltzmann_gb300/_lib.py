@@ -51,6 +51,34 @@ class BatchDesc(C.Structure):
                 ("dt", C.c_double), ("fix_entropy", C.c_int), ("conserve", C.c_int)]
 
 
+class ServerDesc(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_double), ("scheme", C.c_int), ("dt", C.c_double),
+                ("fix_entropy", C.c_int), ("conserve", C.c_int), ("filter", C.c_int),
+                ("max_live_per_group", C.c_int)]
+
+
+class Request(C.Structure):
+    _fields_ = [("N", C.c_int), ("gamma", C.c_double), ("R", C.c_double), ("steps", C.c_int),
+                ("arrival_s", C.c_double), ("want_result", C.c_int)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("state", C.c_int), ("N", C.c_int), ("steps", C.c_int), ("t_arrival", C.c_double),
+                ("t_admit", C.c_double), ("t_done", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("live", C.c_longlong),
+                ("queued", C.c_longlong), ("tts_p50_s", C.c_double), ("tts_p99_s", C.c_double),
+                ("tts_mean_s", C.c_double), ("tts_max_s", C.c_double), ("wait_p50_s", C.c_double),
+                ("wait_p99_s", C.c_double), ("first_arrival_s", C.c_double),
+                ("last_done_s", C.c_double), ("throughput_rps", C.c_double),
+                ("qhat_evals", C.c_double), ("qhat_evals_padded", C.c_double),
+                ("qhat_evals_per_s", C.c_double), ("steps_launched", C.c_longlong),
+                ("kernel_launches", C.c_longlong), ("hbm_bytes_peak", C.c_double),
+                ("groups", C.c_int)]
+
+
 _dp = C.POINTER(C.c_double)
 _fp = C.POINTER(C.c_float)
 _vp = C.c_void_p
@@ -107,6 +135,14 @@ def _load():
         "edb_batch_read": (C.c_int, [_vp, _dp, _dp]),
         "edb_batch_moments": (C.c_int, [_vp, _dp, _dp]),
         "edb_batch_launches_per_step": (C.c_int, [_vp, _ip]),
+        "edb_qcalc_genB_f32": (C.c_int, [_vp]),
+        "edb_server_create": (C.c_int, [C.POINTER(ServerDesc), C.POINTER(_vp)]),
+        "edb_server_destroy": (C.c_int, [_vp]),
+        "edb_server_prepare": (C.c_int, [_vp, C.c_int, C.c_double, C.c_double]),
+        "edb_server_submit": (C.c_int, [_vp, C.POINTER(Request), _dp, C.POINTER(C.c_longlong)]),
+        "edb_server_run": (C.c_int, [_vp, C.c_double]),
+        "edb_server_result": (C.c_int, [_vp, C.c_longlong, _dp, _dp, C.POINTER(RequestInfo)]),
+        "edb_server_get_stats": (C.c_int, [_vp, C.POINTER(ServerStats)]),
         "edb_moments_hat_device": (C.c_int, [C.c_int, C.c_int, C.c_double, _vp, _vp, _vp]),
         "edb_moments_project_device": (C.c_int, [C.c_int, C.c_int, C.c_double, _vp, _vp, _vp]),
         "edb_maxwellian_fit_device": (C.c_int, [C.c_int, C.c_int, C.c_double, _vp, _vp, _vp,

@@ -14,7 +14,8 @@ import numpy as np
 
 from ._lib import (INDEX_REFERENCE, R_REFERENCE, SCHEME_CFE, SCHEME_DUFORT, SCHEME_FE,
                    SCHEME_RK2, SCHEME_RK4, SCHEME_SSP3, BatchDesc, QCalcDesc, QCalcInfo,
-                   SolverDesc, check, devptr, dptr, lib, stream_ptr)
+                   Request, RequestInfo, ServerDesc, ServerStats, SolverDesc, check, devptr, dptr,
+                   lib, stream_ptr)
 
 
 def device_status(clear: bool = True) -> int:
@@ -370,6 +371,80 @@ class BatchSolver:
             if self._h:
                 lib.edb_batch_destroy(self._h)
                 self._h = None
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------- serving engine
+
+class Server:
+    """Device-resident request loop with continuous batching (no reference
+    counterpart).  Requests are independent solves grouped by kernel table
+    (N, gamma, R); all use the server's scheme and dt.  See include/edb.h."""
+
+    def __init__(self, hbm_budget_bytes: float = 80e9, scheme: int = SCHEME_RK4, dt: float = 0.01,
+                 fix_entropy: bool = False, conserve: bool = False, filter: bool = False,
+                 max_live_per_group: int = 0):
+        d = ServerDesc()
+        d.hbm_budget_bytes = float(hbm_budget_bytes)
+        d.scheme = int(scheme)
+        d.dt = float(dt)
+        d.fix_entropy = int(bool(fix_entropy))
+        d.conserve = int(bool(conserve))
+        d.filter = int(bool(filter))
+        d.max_live_per_group = int(max_live_per_group)
+        h = C.c_void_p()
+        check(lib.edb_server_create(C.byref(d), C.byref(h)))
+        self._h = h
+        self._N = {}
+
+    def prepare(self, N: int, gamma: float, R: float):
+        check(lib.edb_server_prepare(self._h, int(N), float(gamma), float(R)))
+
+    def submit(self, N: int, gamma: float, R: float, steps: int, F0_real, arrival_s: float = -1.0,
+               want_result: bool = False) -> int:
+        F0 = np.ascontiguousarray(F0_real, dtype=np.float64).reshape(-1)
+        if F0.size != N ** 3:
+            raise ValueError("expected N^3 real values")
+        r = Request()
+        r.N, r.gamma, r.R, r.steps = int(N), float(gamma), float(R), int(steps)
+        r.arrival_s = float(arrival_s)
+        r.want_result = int(bool(want_result))
+        rid = C.c_longlong()
+        check(lib.edb_server_submit(self._h, C.byref(r), dptr(F0), C.byref(rid)))
+        self._N[rid.value] = int(N)
+        return rid.value
+
+    def run(self, max_wall_s: float = 0.0):
+        check(lib.edb_server_run(self._h, float(max_wall_s)))
+
+    def info(self, rid: int) -> dict:
+        i = RequestInfo()
+        check(lib.edb_server_result(self._h, int(rid), None, None, C.byref(i)))
+        return {"state": i.state, "N": i.N, "steps": i.steps, "t_arrival": i.t_arrival,
+                "t_admit": i.t_admit, "t_done": i.t_done}
+
+    def result(self, rid: int):
+        """(f real N^3, Fhat complex N^3) of a finished request kept with want_result."""
+        NQ = self._N[int(rid)] ** 3
+        F = np.empty(NQ)
+        Fh = np.empty(NQ, dtype=np.complex128)
+        check(lib.edb_server_result(self._h, int(rid), dptr(F), dptr(Fh.view(np.float64)), None))
+        return F, Fh
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        check(lib.edb_server_get_stats(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib.edb_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
 

@@ -31,6 +31,7 @@ UNITS = {
     "edb_kernels_genb.cu": ["-fmad=false"],
     "edb_kernels_misc.cu": ["-fmad=false"],
     "edb_noalloc.cu": [],
+    "edb_server.cu": [],
 }
 
 

@@ -254,6 +254,50 @@ extern "C" edb_status edb_qcalc_genB(edb_qcalc *q) {
   return qcalc_tune_fp64(q);
 }
 
+extern "C" edb_status edb_qcalc_genB_f32(edb_qcalc *q) {
+  if (!q) return fail(EDB_EINVAL, "null handle");
+  if (q->d.index_mode != EDB_INDEX_ALIASED)
+    return fail(EDB_EINVAL, "the FP32 table exists in ALIASED mode only");
+  const int N = q->d.N;
+  const long long NQ = q->p.NQ;
+  const int amax = amax_of(N);
+  if (!q->B32) EDB_TRY(dalloc(&q->B32, (size_t)NQ * NQ + 64));  // +64: masked tail reads
+  double *T = nullptr, *sigma = nullptr, *Bmm = nullptr;
+  edb_status s = dalloc(&T, (size_t)(amax + 1) * (amax + 1));
+  if (s == EDB_OK) s = dalloc(&sigma, 64);
+  if (s == EDB_OK) s = dalloc(&Bmm, (size_t)NQ);
+  if (s == EDB_OK) s = launch_ftable(N, q->d.gamma, T, amax, q->st);
+  if (s == EDB_OK)
+    s = launch_bmm(N, q->d.gamma, q->d.L, q->d.filter, q->d.index_mode, T, amax, sigma, Bmm,
+                   q->st);
+  if (s == EDB_OK)
+    s = launch_genB(N, q->d.gamma, q->d.L, q->d.filter, q->d.index_mode, T, amax, sigma, Bmm,
+                    nullptr, q->B32, q->st);
+  cudaError_t e = cudaStreamSynchronize(q->st);
+  dfree(T);
+  dfree(sigma);
+  dfree(Bmm);
+  if (s != EDB_OK) return s;
+  if (e != cudaSuccess) return cuda_fail(e, "genB_f32");
+  return EDB_OK;
+}
+
+namespace edb {
+const float *qcalc_B32(const edb_qcalc *q) { return q->B32; }
+int qcalc_c32_variant(const edb_qcalc *q, int S, bool *tuned) {
+  if (tuned) *tuned = q->c32_variant[s_bucket(S)] >= 0;
+  return c32_variant_for(q, S);
+}
+long long qcalc_table_bytes(const edb_qcalc *q) {
+  long long b = 0;
+  const long long e = q->p.NQ * q->p.NQ;
+  if (q->B64) b += e * 8;
+  if (q->B2) b += e * 8;
+  if (q->B32) b += e * 4 + 256;
+  return b;
+}
+}  // namespace edb
+
 extern "C" edb_status edb_qcalc_set_B(edb_qcalc *q, const double *host_B) {
   if (!q || !host_B) return fail(EDB_EINVAL, "null argument");
   const long long NQ = q->p.NQ;
@@ -330,7 +374,7 @@ extern "C" edb_status edb_qcalc_calQ_batch_f32_device(edb_qcalc *q, int S, const
   if (S < 1) return fail(EDB_EINVAL, "S must be positive");
   if (q->d.index_mode != EDB_INDEX_ALIASED)
     return fail(EDB_EINVAL, "the batched path runs the ALIASED index mode");
-  if (!q->ready || !q->B32) return fail(EDB_ENOTREADY, "batched calQ before genB");
+  if (!q->B32) return fail(EDB_ENOTREADY, "batched calQ before genB");
   return launch_calq32_batch(q->d.N, S, q->B32, (const float2 *)d_fin, (float2 *)d_Qout,
                              (cudaStream_t)stream, c32_variant_for(q, S));
 }
@@ -342,7 +386,7 @@ extern "C" edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float 
                                                float *d_Qout, void *stream, int *chosen) {
   if (!q || !d_fin || !d_Qout) return fail(EDB_EINVAL, "null argument");
   if (S < 1) return fail(EDB_EINVAL, "S must be positive");
-  if (!q->ready || !q->B32) return fail(EDB_ENOTREADY, "autotune before genB (ALIASED)");
+  if (!q->B32) return fail(EDB_ENOTREADY, "autotune before genB (ALIASED)");
   cudaStream_t st = (cudaStream_t)stream;
   cudaEvent_t e0, e1;
   EDB_CUDA(cudaEventCreate(&e0));

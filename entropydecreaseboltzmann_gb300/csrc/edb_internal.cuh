@@ -163,6 +163,14 @@ edb_status launch_sinusoid_init(int N, double R, double2 *d_F, cudaStream_t st);
 edb_status launch_moments(int N, int batch, double R, const double2 *d_F, double *d_out,
                           cudaStream_t st);
 
+// ---- QCalculator internals used by the serving engine (edb_capi.cu)
+const float *qcalc_B32(const edb_qcalc *q);
+// Batched-kernel variant for S solves; *tuned = false when S's size class has
+// not been autotuned yet.
+int qcalc_c32_variant(const edb_qcalc *q, int S, bool *tuned);
+// Device bytes held by the handle's tables.
+long long qcalc_table_bytes(const edb_qcalc *q);
+
 // ---- conservation (edb_kernels_conserve.cu)
 // Table per (N, R): W1, W2 (N complex each), G^-1 (25), h^3.
 inline int conserve_table_len(int N) { return 4 * N + 32; }

@@ -217,8 +217,8 @@ edb_status launch_bmm(int N, double gamma, double L, int filter, int mode, const
 }
 
 // One CTA per row l (centred); columns k over all N^3 centred modes.
-// Writes B64[l][k] and, when B32 is given, the same value as float at the
-// FFTW-order position [lf][kf] (lf = (l - n) mod N per dimension).
+// Writes B64[l][k] (when given) and, when B32 is given, the same value as
+// float at the FFTW-order position [lf][kf] (lf = (l - n) mod N per dimension).
 __global__ void genB_kernel(int N, int filter, double rval, const double *__restrict__ T, int amax,
                             const double *__restrict__ sigma, const double *__restrict__ Bmm,
                             double *__restrict__ B64, float *__restrict__ B32) {
@@ -247,7 +247,7 @@ __global__ void genB_kernel(int N, int filter, double rval, const double *__rest
     double sigmam = filter ? sigma[m1] * sigma[m2] * sigma[m3] : 1.0;
     long long m = ((long long)m1 * N + m2) * N + m3;
     double v = T[(long long)a * W + b] * sigmal * sigmam * rval - Bmm[m];
-    B64[lc * NQ + kc] = v;
+    if (B64) B64[lc * NQ + kc] = v;
     if (B32) {
       long long kf = ((long long)((k1 - n + N) % N) * N + (k2 - n + N) % N) * N + (k3 - n + N) % N;
       B32[lf * NQ + kf] = (float)v;

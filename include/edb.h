@@ -113,6 +113,11 @@ edb_status edb_qcalc_close_filter(edb_qcalc *q);
  * F_gamma = int_0^1 r^(2+gamma) sinc(xi r) sinc(eta r) dr (ReadMe.md:51). */
 edb_status edb_qcalc_genB(edb_qcalc *q);
 
+/* genB for batched use only (ALIASED mode): builds just the FP32 FFTW-order
+ * table (4 bytes per entry instead of 8 + 8 + 4), so many tables fit in one
+ * HBM budget.  The FP64 calQ entry points then report EDB_ENOTREADY. */
+edb_status edb_qcalc_genB_f32(edb_qcalc *q);
+
 /* virtual calQ(Qout, fin) (QCalculator.h:59, 231-257): FP64, host buffers,
  * synchronous.  fin and Qout hold N^3 interleaved complex doubles. */
 edb_status edb_qcalc_calQ(edb_qcalc *q, const double *fin, double *Qout);
@@ -270,6 +275,80 @@ edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat);
 edb_status edb_batch_moments(edb_batch *b, double *moments, double *entropy);
 /* Kernel launches per step of the captured graph. */
 edb_status edb_batch_launches_per_step(edb_batch *b, int *n);
+
+/* ------------------------------------------------------ serving engine */
+/* No reference counterpart (the reference runs one solve per process).  A
+ * device-resident request loop for many independent solves:
+ *  - requests are grouped by kernel table (N, gamma, R); each group owns one
+ *    FP32 table (edb_qcalc_genB_f32) and a solve arena in HBM;
+ *  - a request is admitted at its group's next step boundary when its slot
+ *    fits the HBM budget (tables + arenas) and the group's live-solve cap;
+ *  - every live solve of a group advances one step per replay of a captured
+ *    CUDA graph (one graph per bucket of 16 live solves); groups run on their
+ *    own streams, so their work overlaps on the device;
+ *  - finished solves are copied out and the arena is compacted, so requests
+ *    that arrive while others run join without waiting for them (continuous
+ *    batching).
+ * Each solve's arithmetic is independent of the others in its batch. */
+typedef struct {
+  double hbm_budget_bytes; /* device bytes for tables plus solve arenas */
+  int scheme;              /* EDB_SCHEME_FE, EDB_SCHEME_SSP3 or EDB_SCHEME_RK4 (all requests) */
+  double dt;
+  int fix_entropy;         /* entropy rule after each step, as edb_batch_desc */
+  int conserve;            /* conservative mode, as edb_batch_desc */
+  int filter;              /* filter of the kernel tables (1 = the reference default) */
+  int max_live_per_group;  /* cap of live solves per group (bounds one step's time); 0 = no cap */
+} edb_server_desc;
+
+typedef struct {
+  int N;              /* modes per dimension */
+  double gamma;       /* VHS exponent of the kernel table */
+  double R;           /* velocity box half-width (also the table's L) */
+  int steps;          /* steps to advance */
+  double arrival_s;   /* arrival on the server clock (seconds since the first
+                         edb_server_run); < 0: arrives when submitted */
+  int want_result;    /* 1: keep f (real space) and Fhat for edb_server_result */
+} edb_request;
+
+typedef struct {
+  int state;          /* 0 queued, 1 running, 2 done */
+  int N, steps;
+  double t_arrival, t_admit, t_done; /* server clock, seconds (-1: not yet) */
+} edb_request_info;
+
+typedef struct {
+  long long submitted, completed, live, queued;
+  double tts_p50_s, tts_p99_s, tts_mean_s, tts_max_s; /* time to solution: arrival -> result */
+  double wait_p50_s, wait_p99_s;                       /* arrival -> admission */
+  double first_arrival_s, last_done_s;                 /* server clock */
+  double throughput_rps;      /* completed / (last_done - first_arrival) */
+  double qhat_evals;          /* Q-hat evaluations of live solves */
+  double qhat_evals_padded;   /* including the padding of 16-solve buckets */
+  double qhat_evals_per_s;    /* qhat_evals / (last_done - first_arrival) */
+  long long steps_launched;   /* graph replays */
+  long long kernel_launches;  /* kernels in those replays plus admission/retirement work */
+  double hbm_bytes_peak;      /* tables + arenas */
+  int groups;
+} edb_server_stats;
+
+typedef struct edb_server edb_server;
+edb_status edb_server_create(const edb_server_desc *d, edb_server **out);
+edb_status edb_server_destroy(edb_server *s);
+/* Builds the table of group (N, gamma, R) now (otherwise the first request of
+ * the group pays for it). */
+edb_status edb_server_prepare(edb_server *s, int N, double gamma, double R);
+/* Queues a request; F0_real (N^3 doubles, host) is copied.  EDB_ENOMEM when
+ * its table plus one slot can never fit the budget. */
+edb_status edb_server_submit(edb_server *s, const edb_request *r, const double *F0_real,
+                             long long *id);
+/* Runs the request loop until every submitted request is done or
+ * max_wall_s seconds (<= 0: no limit) have passed. */
+edb_status edb_server_run(edb_server *s, double max_wall_s);
+/* f (N^3 doubles) and Fhat (N^3 complex) of a finished request kept with
+ * want_result (either pointer may be NULL); info may be NULL. */
+edb_status edb_server_result(edb_server *s, long long id, double *F_real, double *Fhat,
+                             edb_request_info *info);
+edb_status edb_server_get_stats(edb_server *s, edb_server_stats *out);
 
 /* -------------------------------------------------------- conservation */
 /* No reference counterpart: the moment functionals of conservative mode.

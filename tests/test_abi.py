@@ -88,3 +88,36 @@ def test_python_mirror_has_reference_names():
         assert hasattr(e.EntropyFix, name)
     for name in ("FEuler", "CFE", "RK2", "SSP3", "RK4", "DUFORT", "setFixEntropy"):
         assert hasattr(e.BKW3D, name)
+
+
+def test_ctypes_structs_match_header_layout(tmp_path):
+    """Every ctypes mirror of a header struct has the C compiler's size and
+    field offsets (compiled here from include/edb.h)."""
+    import shutil
+    import subprocess
+
+    from entropydecreaseboltzmann_gb300 import _lib
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    mirrors = {"edb_qcalc_desc": _lib.QCalcDesc, "edb_qcalc_info": _lib.QCalcInfo,
+               "edb_solver_desc": _lib.SolverDesc, "edb_batch_desc": _lib.BatchDesc,
+               "edb_server_desc": _lib.ServerDesc, "edb_request": _lib.Request,
+               "edb_request_info": _lib.RequestInfo, "edb_server_stats": _lib.ServerStats}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "edb.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in mirrors.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)

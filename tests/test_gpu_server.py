@@ -1,0 +1,158 @@
+"""Serving engine on the GPU: continuous batching of independent solves.
+
+Stated tolerance for "the same alone and in the mix": relative L2 of f and
+Fhat <= 1e-12 (each solve's arithmetic depends only on its own slot; the
+test also reports whether the results are bit-identical).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def edb():
+    import entropydecreaseboltzmann_gb300 as e
+
+    return e
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_result_same_alone_and_in_mix(edb):
+    from entropydecreaseboltzmann_gb300 import data
+
+    N, R, steps = 16, 6.0, 30
+    f_probe = data.maxwellian_mixture_batch(1, N, R, seed=11)[0]
+    # alone
+    srv = edb.Server(hbm_budget_bytes=8e9, scheme=edb.SCHEME_RK4, dt=0.01)
+    rid = srv.submit(N, 0.0, R, steps, f_probe, want_result=True)
+    srv.run()
+    F_alone, Fh_alone = srv.result(rid)
+    srv.close()
+    # in a mix: other N, gamma and horizons, arrivals spread over the run so
+    # requests join while others are on the GPU
+    rng = np.random.default_rng(5)
+    srv = edb.Server(hbm_budget_bytes=8e9, scheme=edb.SCHEME_RK4, dt=0.01)
+    srv.prepare(N, 0.0, R)
+    srv.prepare(12, 1.0, 6.0)
+    ids = []
+    for j in range(40):
+        n = int(rng.choice([12, 16]))
+        g = float(rng.choice([0.0, 1.0]))
+        f = data.maxwellian_mixture_batch(1, n, 6.0, seed=100 + j)[0]
+        ids.append(srv.submit(n, g, 6.0, int(rng.integers(5, 60)), f,
+                              arrival_s=float(rng.uniform(0, 0.05))))
+    rid = srv.submit(N, 0.0, R, steps, f_probe, arrival_s=0.02, want_result=True)
+    srv.run()
+    F_mix, Fh_mix = srv.result(rid)
+    st = srv.stats()
+    assert st["completed"] == 41
+    assert rel_l2(F_mix, F_alone) <= 1e-12
+    assert rel_l2(Fh_mix, Fh_alone) <= 1e-12
+    print("bit-identical:", bool(np.array_equal(F_mix, F_alone)))
+    srv.close()
+
+
+def test_server_matches_batch_solver(edb):
+    """A served request equals the same solve in a BatchSolver (same scheme,
+    table and FP32-compensated kernel)."""
+    from entropydecreaseboltzmann_gb300 import data
+    from oracle.oracle import INDEX_ALIASED
+
+    N, R, steps = 12, 6.0, 20
+    f0 = data.maxwellian_mixture_batch(3, N, R, seed=21)
+    q = edb.QCalculator(N, 1, L=R, filter=False, index_mode=INDEX_ALIASED)
+    q.genB()
+    b = edb.BatchSolver(q, 3, R, edb.SCHEME_SSP3, 0.005, fix_entropy=True)
+    b.load(f0)
+    b.step(steps)
+    F_b = b.read(real=True)
+    srv = edb.Server(hbm_budget_bytes=4e9, scheme=edb.SCHEME_SSP3, dt=0.005, fix_entropy=True)
+    ids = [srv.submit(N, 1.0, R, steps, f0[i], want_result=True) for i in range(3)]
+    srv.run()
+    for i, rid in enumerate(ids):
+        F, _ = srv.result(rid)
+        assert rel_l2(F, F_b[i]) <= 1e-12
+
+
+def test_served_bkw_accuracy(edb):
+    """BKW requests (Maxwell molecules, N = 24, L = 7, RK4 dt = 0.01, 50
+    steps) served beside other traffic: L-inf <= 1e-6 against the exact BKW
+    solution."""
+    from entropydecreaseboltzmann_gb300 import data
+
+    N, R, dt, steps = 24, 7.0, 0.01, 50
+    t0 = [5.5, 6.5, 7.5]
+    srv = edb.Server(hbm_budget_bytes=12e9, scheme=edb.SCHEME_RK4, dt=dt)
+    ids = [srv.submit(N, 0.0, R, steps, data.bkw_grid(N, R, t), want_result=True) for t in t0]
+    for j in range(6):
+        srv.submit(16, 1.0, 6.0, 30, data.maxwellian_mixture_batch(1, 16, 6.0, seed=j)[0])
+    srv.run()
+    for t, rid in zip(t0, ids):
+        F, _ = srv.result(rid)
+        err = float(np.max(np.abs(F - data.bkw_grid(N, R, t + steps * dt))))
+        assert err <= 1e-6, err
+    assert edb.device_status() == 0
+
+
+def test_continuous_admission_and_budget(edb):
+    """A request arriving while a long one runs is admitted at the next step
+    boundary (it does not wait for the long one to finish); with a budget that
+    holds only a few slots every request still completes."""
+    from entropydecreaseboltzmann_gb300 import data
+
+    N, R = 12, 6.0
+    f = data.maxwellian_mixture_batch(1, N, R, seed=3)[0]
+    srv = edb.Server(hbm_budget_bytes=4e9, scheme=edb.SCHEME_RK4, dt=0.01)
+    srv.prepare(N, 0.0, R)
+    long_id = srv.submit(N, 0.0, R, 400, f)
+    late_id = srv.submit(N, 0.0, R, 5, f, arrival_s=0.05)
+    srv.run()
+    a, b = srv.info(long_id), srv.info(late_id)
+    assert b["t_admit"] < a["t_done"] and b["t_done"] < a["t_done"]
+    assert b["t_admit"] - b["t_arrival"] < 0.5 * (a["t_done"] - a["t_admit"])
+    st = srv.stats()
+    assert st["completed"] == 2 and st["tts_p50_s"] <= st["tts_p99_s"]
+    srv.close()
+    # a budget of one table (N^6 x 4 B = 11.9 MB), its transfer staging
+    # (64 x N^3 x 40 B = 4.4 MB) and about 36 slots (N^3 x 120 B each, RK4),
+    # so the 70 requests are served in waves of whole 16-solve buckets
+    srv = edb.Server(hbm_budget_bytes=2.4e7, scheme=edb.SCHEME_RK4, dt=0.01)
+    for j in range(70):
+        srv.submit(N, 0.0, R, 3, f)
+    srv.run()
+    st = srv.stats()
+    assert st["completed"] == 70
+    assert st["hbm_bytes_peak"] <= 2.4e7
+    srv.close()
+    # a request that can never fit is refused at submission
+    srv = edb.Server(hbm_budget_bytes=1.0e6, scheme=edb.SCHEME_RK4, dt=0.01)
+    with pytest.raises(edb.EdbError) as ei:
+        srv.submit(N, 0.0, R, 3, f)
+    assert ei.value.status == 2  # EDB_ENOMEM
+    srv.close()
+
+
+def test_conservative_serving(edb):
+    """Conservative mode through the server: moments of each served solve
+    kept to 1e-10 relative."""
+    from entropydecreaseboltzmann_gb300 import data
+
+    N, R = 12, 6.0
+    f0 = data.maxwellian_mixture_batch(4, N, R, seed=31)
+    srv = edb.Server(hbm_budget_bytes=4e9, scheme=edb.SCHEME_SSP3, dt=0.005, fix_entropy=True,
+                     conserve=True)
+    ids = [srv.submit(N, 1.0, R, 25 + 5 * i, f0[i], want_result=True) for i in range(4)]
+    srv.run()
+    h = 2 * R / N
+    x = -R + h * np.arange(N)
+    X, Y, Z = [a.reshape(-1) for a in np.meshgrid(x, x, x, indexing="ij")]
+    phi = np.stack([np.ones_like(X), X, Y, Z, X * X + Y * Y + Z * Z])
+    for i, rid in enumerate(ids):
+        F, _ = srv.result(rid)
+        m, m0 = phi @ F * h ** 3, phi @ f0[i] * h ** 3
+        sc = np.array([m0[0], *(3 * [np.sqrt(m0[0] * m0[4])]), m0[4]])
+        assert np.max(np.abs(m - m0) / sc) <= 1e-10
