@@ -12,8 +12,14 @@ with host buffers — per step, edb_batch_load (pinned host real-space f in,
 forward FFT), one RK4 step, edb_batch_read (inverse FFT, real-space f out).
 Also reported: the FP64 drop-in single-solve path at N = 24 and N = 32
 (evals/s and B-stream bandwidth), the BKW L-infinity error of the batched
-FP32 path after 50 RK4 steps, the roofline of the dominant kernel and the
-CPU baseline (the oracle's restatement of QCalculator::calQ on host threads).
+FP32 path after 50 RK4 steps, the roofline of the dominant kernel, the
+CPU baseline (the oracle's restatement of QCalculator::calQ on host threads)
+and the serving engine on the serving-stream mix (N in {16, 24, 32} with
+probabilities 0.5/0.3/0.2, gamma in {0, 1}, horizons log-uniform in [20, 500]
+RK4 steps, 5% BKW requests, 80 GB budget): its capacity (all requests at
+once) and p50/p99 time-to-solution under Poisson arrivals at 70% of that
+capacity.  --uneven adds the uneven batch (512 solves each at N = 16, 24,
+32, gamma in {0, 0.5, 1}, SSP3 dt = 0.005, U{20..200} steps).
 
 Usage:  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 For N > 1 (torchrun) every rank runs an independent replica of the workload
@@ -199,6 +205,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", type=int, default=S_BATCH)
+    ap.add_argument("--serve-requests", type=int, default=600,
+                    help="request pool of the capacity run (0: skip serving)")
+    ap.add_argument("--serve-capacity-seconds", type=float, default=20.0,
+                    help="window of the steady-state capacity run")
+    ap.add_argument("--serve-seconds", type=float, default=20.0,
+                    help="arrival window of the Poisson run")
+    ap.add_argument("--uneven", action="store_true", help="also run the uneven batch")
+    ap.add_argument("--uneven-per-n", type=int, default=512)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -340,6 +354,11 @@ def main():
     exact = np.stack([data.bkw_grid(N, L_BOX, t + 50 * DT) for t in t0b])
     bkw_linf = float(np.max(np.abs(fend - exact)))
 
+    del bb, bs
+    torch.cuda.synchronize()
+    serve = run_serving(edb, args, rank) if args.serve_requests > 0 else None
+    uneven = run_uneven(edb, args, rank) if args.uneven else None
+
     line = None
     if rank == 0:
         cpu = None if args.no_cpu_baseline else cpu_baseline()
@@ -365,13 +384,81 @@ def main():
             "fp64_dropin": fp64, "hbm_peak_GBs": peaks["hbm_gbs"], "hbm_peak_source": peak_src,
             "batched_over_fp64_N24": value / fp64["N24"]["emulated"]["evals_per_s"],
             "bkw_linf_fp32_50_steps": bkw_linf,
+            "serve": serve,
             "cpu_baseline": cpu,
         }
+        if uneven is not None:
+            line["uneven_batch"] = uneven
         print(json.dumps(line), flush=True)
     if pg is not None:
         pg.barrier()
         pg.destroy_process_group()
     return 0
+
+
+SERVE_KEYS = ("completed", "tts_p50_s", "tts_p99_s", "tts_mean_s", "tts_max_s", "wait_p50_s",
+              "wait_p99_s", "throughput_rps", "qhat_evals_per_s", "qhat_evals",
+              "qhat_evals_padded", "steps_launched", "kernel_launches", "groups")
+
+
+def run_serving(edb, args, rank):
+    """Serving-stream mix through edb.Server: steady-state capacity with a
+    fixed number of requests in flight, then Poisson arrivals at 70% of it
+    (all requests run to completion; times are on the server clock, host
+    data in and out)."""
+    from entropydecreaseboltzmann_gb300 import serving
+
+    budget = 80e9
+    srv = edb.Server(hbm_budget_bytes=budget, scheme=edb.SCHEME_RK4, dt=DT)
+    pool = serving.stream_requests(rate=1e6, duration=args.serve_requests * 1e-6 * 4,
+                                   seed=3000 + rank)
+    capacity, cap_evals, cap_pad, ncap = serving.measure_capacity(
+        srv, pool, concurrency=96, seconds=args.serve_capacity_seconds)
+    srv.close()
+    rate = 0.7 * capacity
+    srv = edb.Server(hbm_budget_bytes=budget, scheme=edb.SCHEME_RK4, dt=DT)
+    reqs = serving.stream_requests(rate=rate, duration=args.serve_seconds, seed=4000 + rank)
+    st, _ = serving.run(srv, reqs, DT)
+    srv.close()
+    gpu_s_per_req = 1.0 / capacity
+    out = {
+        "workload": "serving stream: N 16/24/32 (p .5/.3/.2, L 6/7/8), gamma {0,1}, mixture of "
+                    "1-3 Maxwellians, 5% BKW, horizon log-U[20,500] RK4 steps dt=0.01, 80 GB "
+                    "HBM budget; tables built before the clock starts",
+        "capacity_rps": capacity,
+        "capacity_run": {"in_flight": 96, "window_s": args.serve_capacity_seconds,
+                         "completions_counted": ncap, "qhat_evals_per_s": cap_evals,
+                         "padding_overhead": cap_pad},
+        "offered_rps": rate,
+        "arrival_window_s": args.serve_seconds,
+        "requests": st["submitted"],
+        "hbm_peak_GB": st["hbm_bytes_peak"] / 1e9,
+        "bkw_linf_by_N": st["bkw_linf_by_N"],
+        "bkw_requests": st["bkw_requests"],
+        "padding_overhead": st["qhat_evals_padded"] / max(st["qhat_evals"], 1.0),
+        "note": (f"one GPU sustains {capacity:.1f} req/s of this mix ({gpu_s_per_req * 1e3:.0f} "
+                 f"GPU-ms per request), so 2000 req/s would need {2000 * gpu_s_per_req:.0f} GPUs; "
+                 f"p50/p99 are reported at a sustained 70% of the measured capacity"),
+    }
+    out.update({k: st[k] for k in SERVE_KEYS})
+    return out
+
+
+def run_uneven(edb, args, rank):
+    """Uneven batch: every request at t = 0, 9 kernel tables, SSP3 with the
+    moment-preserving entropy fix (conservative mode)."""
+    from entropydecreaseboltzmann_gb300 import serving
+
+    srv = edb.Server(hbm_budget_bytes=80e9, scheme=edb.SCHEME_SSP3, dt=0.005, fix_entropy=True,
+                     conserve=True)
+    reqs = serving.uneven_requests(args.uneven_per_n, seed=5000 + rank)
+    st, _ = serving.run(srv, reqs, 0.005)
+    srv.close()
+    out = {"workload": f"uneven batch: {args.uneven_per_n} solves each at N=16/24/32 (L 6/7/8), "
+                       "gamma U{0,0.5,1}, SSP3 dt=0.005, U{20..200} steps, fix on, conservative",
+           "makespan_s": st["last_done_s"], "hbm_peak_GB": st["hbm_bytes_peak"] / 1e9}
+    out.update({k: st[k] for k in SERVE_KEYS})
+    return out
 
 
 def C_double_peak(edb):

@@ -106,6 +106,8 @@ def _load():
         "edb_qcalc_calQ": (C.c_int, [_vp, _dp, _dp]),
         "edb_qcalc_calQ_device": (C.c_int, [_vp, _vp, _vp, _vp]),
         "edb_qcalc_calQ_batch_f32_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
+        "edb_qcalc_calQ_batch_f32_ex": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp,
+                                                  _vp]),
         "edb_qcalc_autotune_batch": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _ip]),
         "edb_device_status": (C.c_int, [_ip, C.c_int]),
         "edb_qcalc_set_fp64_kernel": (C.c_int, [_vp, C.c_int]),
@@ -143,6 +145,7 @@ def _load():
         "edb_server_run": (C.c_int, [_vp, C.c_double]),
         "edb_server_result": (C.c_int, [_vp, C.c_longlong, _dp, _dp, C.POINTER(RequestInfo)]),
         "edb_server_get_stats": (C.c_int, [_vp, C.POINTER(ServerStats)]),
+        "edb_server_clock": (C.c_int, [_vp, _dp]),
         "edb_moments_hat_device": (C.c_int, [C.c_int, C.c_int, C.c_double, _vp, _vp, _vp]),
         "edb_moments_project_device": (C.c_int, [C.c_int, C.c_int, C.c_double, _vp, _vp, _vp]),
         "edb_maxwellian_fit_device": (C.c_int, [C.c_int, C.c_int, C.c_double, _vp, _vp, _vp,

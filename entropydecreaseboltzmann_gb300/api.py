@@ -91,6 +91,14 @@ class QCalculator:
         check(lib.edb_qcalc_calQ_batch_f32_device(self._h, int(S), devptr(d_fin), devptr(d_Q),
                                                   stream_ptr(stream)))
 
+    def calQ_batch_f32_ex(self, S, variant, chunks, d_partial, d_fin, d_Q, stream=None):
+        """Batched kernel with an explicit variant (0, 1: 16-solve groups; 2:
+        4-solve groups) and l1-plane chunk count (d_partial: chunks x S x N^3
+        x 16 bytes on the device when chunks > 1)."""
+        check(lib.edb_qcalc_calQ_batch_f32_ex(self._h, int(S), int(variant), int(chunks),
+                                              devptr(d_partial), devptr(d_fin), devptr(d_Q),
+                                              stream_ptr(stream)))
+
     def set_fp64_kernel(self, kind):
         """0 = FP64-accurate double-float on the FP32 pipe (default), 1 = native FP64."""
         check(lib.edb_qcalc_set_fp64_kernel(self._h, int(kind)))
@@ -431,6 +439,12 @@ class Server:
         Fh = np.empty(NQ, dtype=np.complex128)
         check(lib.edb_server_result(self._h, int(rid), dptr(F), dptr(Fh.view(np.float64)), None))
         return F, Fh
+
+    def clock(self) -> float:
+        """Server clock in seconds (0 before the first run)."""
+        t = C.c_double()
+        check(lib.edb_server_clock(self._h, C.byref(t)))
+        return t.value
 
     def stats(self) -> dict:
         st = ServerStats()

@@ -86,14 +86,15 @@ struct edb_qcalc {
   double2 *fin = nullptr, *Q = nullptr;  // host-API staging
   int nchunk = 0;
   bool ready = false;
-  int c32_variant[16];  // autotuned batched-kernel variant per S bucket, -1 = untuned
+  int c32_variant[16];        // autotuned batched-kernel variant per S class, -1 = untuned
+  int c32_variant_split[16];  // the same for chunked launches (serving engine)
 };
 
-// S bucket of the autotuner: floor(log2(number of 16-solve groups)).
+// S class of the autotuner: floor(log2(S)), capped at 15.
 static int s_bucket(int S) {
-  int groups = (S + 15) / 16, b = 0;
-  while (groups > 1 && b < 15) {
-    groups >>= 1;
+  int b = 0;
+  while (S > 1 && b < 15) {
+    S >>= 1;
     ++b;
   }
   return b;
@@ -130,6 +131,7 @@ extern "C" edb_status edb_qcalc_create(const edb_qcalc_desc *d, edb_qcalc **out)
   EDB_TRY(ensure_device());
   edb_qcalc *q = new edb_qcalc();
   for (int &v : q->c32_variant) v = -1;
+  for (int &v : q->c32_variant_split) v = -1;
   q->d = *d;
   q->p = make_qparams(d->N, d->index_mode);
   cudaError_t e = cudaStreamCreateWithFlags(&q->st, cudaStreamNonBlocking);
@@ -284,9 +286,10 @@ extern "C" edb_status edb_qcalc_genB_f32(edb_qcalc *q) {
 
 namespace edb {
 const float *qcalc_B32(const edb_qcalc *q) { return q->B32; }
-int qcalc_c32_variant(const edb_qcalc *q, int S, bool *tuned) {
-  if (tuned) *tuned = q->c32_variant[s_bucket(S)] >= 0;
-  return c32_variant_for(q, S);
+int qcalc_c32_variant(const edb_qcalc *q, int S, bool *tuned, bool split) {
+  const int v = (split ? q->c32_variant_split : q->c32_variant)[s_bucket(S)];
+  if (tuned) *tuned = v >= 0;
+  return v < 0 ? 0 : v;
 }
 long long qcalc_table_bytes(const edb_qcalc *q) {
   long long b = 0;
@@ -382,12 +385,10 @@ extern "C" edb_status edb_qcalc_calQ_batch_f32_device(edb_qcalc *q, int S, const
 // Times every variant of the batched kernel on the caller's buffers (two
 // launches each after one warm-up, CUDA events on `stream`) and keeps the
 // fastest for this S bucket.
-extern "C" edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float *d_fin,
-                                               float *d_Qout, void *stream, int *chosen) {
-  if (!q || !d_fin || !d_Qout) return fail(EDB_EINVAL, "null argument");
-  if (S < 1) return fail(EDB_EINVAL, "S must be positive");
-  if (!q->B32) return fail(EDB_ENOTREADY, "autotune before genB (ALIASED)");
-  cudaStream_t st = (cudaStream_t)stream;
+// Times every variant of the batched kernel on the caller's buffers (chunk
+// count C, partial buffer for C > 1) and records the fastest for S's class.
+static edb_status autotune_c32(edb_qcalc *q, int S, const float2 *d_fin, float2 *d_Qout,
+                               cudaStream_t st, int C, float4 *d_partial, int *chosen) {
   cudaEvent_t e0, e1;
   EDB_CUDA(cudaEventCreate(&e0));
   EDB_CUDA(cudaEventCreate(&e1));
@@ -395,7 +396,8 @@ extern "C" edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float 
   float best_ms = 1e30f;
   edb_status rc = EDB_OK;
   for (int v = 0; v < calq32_variants() && rc == EDB_OK; ++v) {
-    rc = launch_calq32_batch(q->d.N, S, q->B32, (const float2 *)d_fin, (float2 *)d_Qout, st, v);
+    if (calq32_group(v) < 16 && S > 64) continue;  // small groups are for few solves
+    rc = launch_calq32_batch(q->d.N, S, q->B32, d_fin, d_Qout, st, v, C, d_partial);
     if (rc == EDB_EINVAL) {  // this variant does not fit this N: skip it
       rc = EDB_OK;
       continue;
@@ -403,7 +405,7 @@ extern "C" edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float 
     if (rc != EDB_OK) break;
     cudaEventRecord(e0, st);
     for (int r = 0; r < 2 && rc == EDB_OK; ++r)
-      rc = launch_calq32_batch(q->d.N, S, q->B32, (const float2 *)d_fin, (float2 *)d_Qout, st, v);
+      rc = launch_calq32_batch(q->d.N, S, q->B32, d_fin, d_Qout, st, v, C, d_partial);
     cudaEventRecord(e1, st);
     cudaError_t e = cudaEventSynchronize(e1);
     if (e != cudaSuccess) {
@@ -420,9 +422,38 @@ extern "C" edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float 
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc != EDB_OK) return rc;
-  q->c32_variant[s_bucket(S)] = best;
+  (C > 1 ? q->c32_variant_split : q->c32_variant)[s_bucket(S)] = best;
   if (chosen) *chosen = best;
   return EDB_OK;
+}
+
+namespace edb {
+edb_status qcalc_autotune_split(edb_qcalc *q, int S, const float2 *d_fin, float2 *d_Qout,
+                                cudaStream_t st, int C, float4 *d_partial) {
+  return autotune_c32(q, S, d_fin, d_Qout, st, C, d_partial, nullptr);
+}
+}  // namespace edb
+
+extern "C" edb_status edb_qcalc_calQ_batch_f32_ex(edb_qcalc *q, int S, int variant, int chunks,
+                                                  void *d_partial, const float *d_fin,
+                                                  float *d_Qout, void *stream) {
+  if (!q || !d_fin || !d_Qout) return fail(EDB_EINVAL, "null argument");
+  if (S < 1) return fail(EDB_EINVAL, "S must be positive");
+  if (variant < 0 || variant >= calq32_variants()) return fail(EDB_EINVAL, "unknown variant");
+  if (chunks < 1 || chunks > q->d.N) return fail(EDB_EINVAL, "chunks must be in [1, N]");
+  if (chunks > 1 && !d_partial) return fail(EDB_EINVAL, "chunks > 1 need a partial buffer");
+  if (!q->B32) return fail(EDB_ENOTREADY, "batched calQ before genB");
+  return launch_calq32_batch(q->d.N, S, q->B32, (const float2 *)d_fin, (float2 *)d_Qout,
+                             (cudaStream_t)stream, variant, chunks, (float4 *)d_partial);
+}
+
+extern "C" edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float *d_fin,
+                                               float *d_Qout, void *stream, int *chosen) {
+  if (!q || !d_fin || !d_Qout) return fail(EDB_EINVAL, "null argument");
+  if (S < 1) return fail(EDB_EINVAL, "S must be positive");
+  if (!q->B32) return fail(EDB_ENOTREADY, "autotune before genB (ALIASED)");
+  return autotune_c32(q, S, (const float2 *)d_fin, (float2 *)d_Qout, (cudaStream_t)stream, 1,
+                      nullptr, chosen);
 }
 
 extern "C" edb_status edb_device_status(int *status, int clear) {

@@ -106,10 +106,14 @@ edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const float4 *d_
                           double2 *d_partial, double2 *d_Q, cudaStream_t st, int minb);
 
 // Batched FP32 calQ (ALIASED): S solves, B32 in FFTW order.
-// variant in [0, calq32_variants()) selects the CTA-size bound (see the kernel).
+// variant in [0, calq32_variants()) selects the solve group and CTA shape
+// (see the kernel).  C > 1 splits the l1 planes into C chunks reduced in
+// order in FP64; d_partial then holds C * S * N^3 float4.
 int calq32_variants();
+int calq32_group(int variant);  // solves per CTA group
 edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin,
-                               float2 *d_Q, cudaStream_t st, int variant);
+                               float2 *d_Q, cudaStream_t st, int variant, int C = 1,
+                               float4 *d_partial = nullptr);
 // Reads (and optionally clears) the batched kernel's status word: nonzero
 // when a bounded wait inside it ran out.
 edb_status read_calq32_status(int *status, bool clear);
@@ -165,9 +169,12 @@ edb_status launch_moments(int N, int batch, double R, const double2 *d_F, double
 
 // ---- QCalculator internals used by the serving engine (edb_capi.cu)
 const float *qcalc_B32(const edb_qcalc *q);
-// Batched-kernel variant for S solves; *tuned = false when S's size class has
-// not been autotuned yet.
-int qcalc_c32_variant(const edb_qcalc *q, int S, bool *tuned);
+// Batched-kernel variant for S solves (split: chunked launches); *tuned =
+// false when S's size class has not been autotuned yet.
+int qcalc_c32_variant(const edb_qcalc *q, int S, bool *tuned, bool split);
+// Autotunes the chunked launch (C chunks, partial buffer) for S solves.
+edb_status qcalc_autotune_split(edb_qcalc *q, int S, const float2 *d_fin, float2 *d_Qout,
+                                cudaStream_t st, int C, float4 *d_partial);
 // Device bytes held by the handle's tables.
 long long qcalc_table_bytes(const edb_qcalc *q);
 

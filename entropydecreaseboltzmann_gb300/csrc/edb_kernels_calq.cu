@@ -9,6 +9,8 @@
 //
 // Batched FP32 path (many solves sharing one B table, ALIASED mode): see the
 // comment above calq32_kernel.
+#include <algorithm>
+
 #include "edb_internal.cuh"
 
 namespace edb {
@@ -154,9 +156,11 @@ edb_status launch_calq64_reduce(const QParams &p, int nchunk, const double2 *d_p
 // Work: Q^s_K = sum_L B[L][K] f^s_L f^s_((K-L) mod N) for S solves; every index
 // in FFTW order, B32 row-major [L][K].
 //
-// CTA = (group of SG = 16 solves) x (one k1, a tile of K2T k2 values, all k3).
-// Thread = (solve pair {w, w+8}, k2, run of A = 8 consecutive k3).  The CTA
-// walks the l-lines (l1, l2) in order; for each line it needs
+// CTA = (group of SG = 2 WS solves) x (one k1, a tile of K2T k2 values, all
+// k3) x (a chunk of l1 planes).  Thread = (solve pair {w, w+WS}, k2, run of
+// A = 8 consecutive k3).  WS = 8 (16-solve groups) for throughput; WS = 2
+// (4-solve groups) for the few live solves of a serving table.  The CTA walks
+// the l-lines (l1, l2) of its chunk in order; for each line it needs
 //   B[(l1,l2,l3)][k1, k2-tile, all k3]  N rows of K2T*N floats (the B tile),
 //   f^s[l1][l2][:]                       N complex per solve (the f_l line),
 //   f^s[m1][:][:], m1 = k1 - l1          the m1-plane, kept while l1 is fixed.
@@ -181,12 +185,16 @@ edb_status launch_calq64_reduce(const QParams &p, int nchunk, const double2 *d_p
 // registers.  Sums are plain FP32 FMA across FOLD_LINES l-lines (FOLD_LINES * N
 // terms per output), then combined and folded into a (hi, lo) two-sum pair:
 // blocked compensated summation.
+//
+// Chunks: with C > 1 the l1 planes are split into C consecutive chunks so that
+// a few solves still fill the GPU; each chunk writes its (hi, lo) pairs and
+// calq32_reduce_kernel adds the chunks in order in FP64.  The chunk
+// boundaries depend only on (N, C), never on S or the variant, so a solve's
+// result does not depend on what else is in the batch.
 // ---------------------------------------------------------------------------
 namespace {
 constexpr int A = 8;                      // k3 outputs per thread
 constexpr int SC = 2;                     // solves per thread: w and w + WS
-constexpr int WS = 8;                     // solve lanes per (k2, k3-run)
-constexpr int SG = SC * WS;               // solves per CTA
 constexpr int ROWPAD = 8;                 // floats after each B-tile row
 constexpr int FLPAD = 2;                  // complex after each f_l line
 constexpr int PLPAD = 2;                  // complex after each solve's plane
@@ -198,7 +206,7 @@ __device__ int g_calq32_status;  // nonzero: a bounded wait ran out
 constexpr int MAX_ST = 4;                 // pipeline stages (l-lines in flight)
 
 struct C32Geom {
-  int N, R, RA, K2T, BROW, FLS, PSTR, NST, NPL, HLT;
+  int N, R, RA, K2T, BROW, FLS, PSTR, NST, NPL, HLT, SG;
   size_t off_B, off_fl, off_pl, off_hl, bytes;
 };
 
@@ -206,8 +214,9 @@ struct C32Geom {
 // m1-planes and, when HLT > 0, the compensated (hi, lo) sums of HLT threads
 // (2 * A * SC packed pairs each, thread-fastest so accesses never conflict).
 // Barriers: full[MAX_ST], empty[MAX_ST], plane[2].
-__host__ __device__ inline C32Geom c32_geom(int N, int K2T, int NST, int NPL, int HLT) {
+__host__ __device__ inline C32Geom c32_geom(int N, int K2T, int NST, int NPL, int HLT, int SG) {
   C32Geom g;
+  g.SG = SG;
   g.N = N;
   g.R = (N + A - 1) / A;
   g.RA = g.R * A;
@@ -353,7 +362,7 @@ __device__ __forceinline__ void stage_line(const C32Geom &g, int li, int st, int
                                            float2 *fls, uint64_t *full) {
   const int N = g.N;
   float *Bd = Bs + (size_t)st * g.RA * g.BROW;
-  float2 *fd = fls + (size_t)st * SG * g.FLS;
+  float2 *fd = fls + (size_t)st * g.SG * g.FLS;
   const float *Bsrc = B32 + (long long)li * N * NQ + (long long)k1 * N * N + (long long)k2_0 * N;
   const float2 *fsrc = fin + (long long)s0 * NQ + (long long)li * N;
   const int rowlen = k2n * N;
@@ -473,15 +482,18 @@ __device__ __forceinline__ void compute_line(const C32Geom &g, const float *Bt, 
 
 // MAXT bounds the CTA size: 256 threads keep at most two warps per SM
 // sub-partition, so up to 255 registers per thread; 384 allow more warps at
-// 168 registers.  The autotuner picks the variant per (N, S).
-// HLS: keep the compensated (hi, lo) pairs in shared memory instead of
-// registers, which frees 64 registers per thread for more resident warps.
-template <bool TMA, int MAXT, bool HLS>
+// 168 registers.  HLS: keep the compensated (hi, lo) pairs in shared memory
+// instead of registers, which frees 64 registers per thread for more resident
+// warps.  WS: solve lanes (group of 2 WS solves).  The autotuner picks the
+// variant per (table, S).
+template <bool TMA, int MAXT, bool HLS, int WS>
 __global__ void __launch_bounds__(MAXT, 1)
-    calq32_kernel(int N, int S, int K2T, int NST, int NPL, const float *__restrict__ B32,
-                  const float2 *__restrict__ fin, float2 *__restrict__ Q) {
+    calq32_kernel(int N, int S, int K2T, int NST, int NPL, int C, const float *__restrict__ B32,
+                  const float2 *__restrict__ fin, float2 *__restrict__ Q,
+                  float4 *__restrict__ partial) {
+  constexpr int SG = SC * WS;
   extern __shared__ __align__(128) unsigned char smem[];
-  const C32Geom g = c32_geom(N, K2T, NST, NPL, HLS ? (int)blockDim.x : 0);
+  const C32Geom g = c32_geom(N, K2T, NST, NPL, HLS ? (int)blockDim.x : 0, SG);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);  // [MAX_ST]
   uint64_t *empty = full + MAX_ST;                       // [MAX_ST]
   uint64_t *pbar = full + 2 * MAX_ST;                    // [2] planes
@@ -503,9 +515,14 @@ __global__ void __launch_bounds__(MAXT, 1)
   const bool k_ok = (k2l < k2n);
   const int k2c = k_ok ? k2 : k2_0;
   const int k3_0 = r * A;
-  const int s0 = blockIdx.x * SG;
+  const int chunk = blockIdx.x % C;
+  const int s0 = (blockIdx.x / C) * SG;
   const int nval = min(SG, S - s0);
-  const int NL = N * N;  // l-lines
+  // this chunk's l1 planes [P0, P1) and l-lines [li0, li0 + nlines)
+  const int PPC = (N + C - 1) / C;
+  const int P0 = min(N, chunk * PPC), P1 = min(N, P0 + PPC);
+  const int nplanes = P1 - P0;
+  const int li0 = P0 * N, nlines = nplanes * N;
   const size_t plane_sz = (size_t)SG * g.PSTR;
 
   // zero the tile/line buffers once: padded rows (l3 >= N), row tails and the
@@ -544,55 +561,58 @@ __global__ void __launch_bounds__(MAXT, 1)
     }
   const u64 neg_re = pk(-1.f, 1.f);
 
+  // Pipeline bookkeeping uses chunk-relative indices: j (line), pr (plane).
   // prologue: lines 0 .. NST-2 and the first plane
   int issued = 0, planes = 0;  // counted in warp 0
-  if (TMA && warp == 0) {
-    for (int li = 0; li < NST - 1 && li < NL; ++li, ++issued)
-      stage_line<true>(g, li, li % NST, k1, k2_0, k2n, s0, nval, NQ, B32, fin, Bs, fls, full);
-    stage_plane<true>(g, (k1 + N) % N, s0, nval, NQ, fin, plb, &pbar[0]);
+  if (TMA && warp == 0 && nlines > 0) {
+    for (int j = 0; j < NST - 1 && j < nlines; ++j, ++issued)
+      stage_line<true>(g, li0 + j, j % NST, k1, k2_0, k2n, s0, nval, NQ, B32, fin, Bs, fls, full);
+    stage_plane<true>(g, (k1 - P0 + N) % N, s0, nval, NQ, fin, plb, &pbar[0]);
     ++planes;
   }
   bool to = false;
   bool aborted = false;
-  for (int li = 0; li < NL; ++li) {
+  for (int j = 0; j < nlines; ++j) {
+    const int li = li0 + j;
     const int l1 = li / N, l2 = li % N;
-    const int st = li % NST;
-    const int pb = (NPL == 2) ? (l1 & 1) : 0;
+    const int pr = l1 - P0;
+    const int st = j % NST;
+    const int pb = (NPL == 2) ? (pr & 1) : 0;
     if (l2 == 0) {
-      // every warp is done with plane l1-1 (and with its buffer)
+      // every warp is done with the previous plane (and with its buffer)
       if (__syncthreads_or(to)) {
         aborted = true;
         break;
       }
       if (TMA) {
         if (NPL == 2) {
-          if (warp == 0 && l1 + 1 < N) {
+          if (warp == 0 && pr + 1 < nplanes) {
             stage_plane<true>(g, (k1 - (l1 + 1) + N) % N, s0, nval, NQ, fin,
-                              plb + (size_t)((l1 + 1) & 1) * plane_sz, &pbar[(l1 + 1) & 1]);
+                              plb + (size_t)((pr + 1) & 1) * plane_sz, &pbar[(pr + 1) & 1]);
             ++planes;
           }
-          mbar_wait(&pbar[l1 & 1], (uint32_t)((l1 >> 1) & 1), to);
+          mbar_wait(&pbar[pr & 1], (uint32_t)((pr >> 1) & 1), to);
         } else {
-          if (warp == 0 && l1 > 0) {
+          if (warp == 0 && pr > 0) {
             stage_plane<true>(g, (k1 - l1 + N) % N, s0, nval, NQ, fin, plb, &pbar[0]);
             ++planes;
           }
-          mbar_wait(&pbar[0], (uint32_t)(l1 & 1), to);
+          mbar_wait(&pbar[0], (uint32_t)(pr & 1), to);
         }
       } else {
         stage_plane<false>(g, (k1 - l1 + N) % N, s0, nval, NQ, fin, plb, pbar);
       }
     }
     if (TMA) {
-      // refill: line li+NST-1 goes into the stage line li-1 used
-      const int ln = li + NST - 1;
-      if (warp == 0 && ln < NL) {
-        const int sn = ln % NST;
-        if (li >= 1) mbar_wait(&empty[sn], (uint32_t)(((li - 1) / NST) & 1), to);
-        stage_line<true>(g, ln, sn, k1, k2_0, k2n, s0, nval, NQ, B32, fin, Bs, fls, full);
+      // refill: line j+NST-1 goes into the stage line j-1 used
+      const int jn = j + NST - 1;
+      if (warp == 0 && jn < nlines) {
+        const int sn = jn % NST;
+        if (j >= 1) mbar_wait(&empty[sn], (uint32_t)(((j - 1) / NST) & 1), to);
+        stage_line<true>(g, li0 + jn, sn, k1, k2_0, k2n, s0, nval, NQ, B32, fin, Bs, fls, full);
         ++issued;
       }
-      mbar_wait(&full[st], (uint32_t)((li / NST) & 1), to);
+      mbar_wait(&full[st], (uint32_t)((j / NST) & 1), to);
     } else {
       __syncthreads();  // previous line's readers are done (single buffer)
       stage_line<false>(g, li, st, k1, k2_0, k2n, s0, nval, NQ, B32, fin, Bs, fls, full);
@@ -667,7 +687,7 @@ __global__ void __launch_bounds__(MAXT, 1)
   for (int c = 0; c < SC; ++c) {
     const int s = s0 + w + c * WS;
     if (s >= S) continue;
-    float2 *qp = Q + (long long)s * NQ + (long long)k1 * N * N + (long long)k2 * N;
+    const long long o = (long long)k1 * N * N + (long long)k2 * N;
 #pragma unroll
     for (int a = 0; a < A; ++a) {
       const int k3 = k3_0 + a;
@@ -681,39 +701,65 @@ __global__ void __launch_bounds__(MAXT, 1)
           lv = lo[HLS ? 0 : a][c];
         }
         const float2 h = upk(hv), l = upk(lv);
-        qp[k3] = make_float2(h.x + l.x, h.y + l.y);
+        if (C == 1)
+          Q[(long long)s * NQ + o + k3] = make_float2(h.x + l.x, h.y + l.y);
+        else
+          partial[((long long)chunk * S + s) * NQ + o + k3] = make_float4(h.x, h.y, l.x, l.y);
       }
     }
   }
 }
 
+// Chunk reduction: Q = sum over chunks (in order) of hi + lo, in FP64.
+__global__ void calq32_reduce_kernel(long long n, int C, const float4 *__restrict__ partial,
+                                     float2 *__restrict__ Q) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double re = 0.0, im = 0.0;
+    for (int c = 0; c < C; ++c) {
+      const float4 v = partial[(long long)c * n + i];
+      re += (double)v.x + (double)v.z;
+      im += (double)v.y + (double)v.w;
+    }
+    Q[i] = make_float2((float)re, (float)im);
+  }
+}
+
 // Variants the autotuner chooses from:
-//   0: CTA <= 256 threads, (hi, lo) in registers (up to 255 registers/thread)
-//   1: CTA <= 384 threads, (hi, lo) in shared memory (168 registers/thread)
-int calq32_variants() { return 2; }
+//   0: 16-solve groups, CTA <= 256 threads, (hi, lo) in registers (<= 255 registers)
+//   1: 16-solve groups, CTA <= 384 threads, (hi, lo) in shared memory (168 registers)
+//   2: 4-solve groups, CTA <= 256 threads, (hi, lo) in registers
+int calq32_variants() { return 3; }
 
-static int variant_maxt(int v) { return v == 0 ? 256 : 384; }
+static int variant_maxt(int v) { return v == 1 ? 384 : 256; }
+static int variant_ws(int v) { return v == 2 ? 2 : 8; }
+int calq32_group(int variant) { return SC * variant_ws(variant); }
 
-template <bool TMA, int MAXT, bool HLS>
+template <bool TMA, int MAXT, bool HLS, int WS>
 static edb_status launch_c32(dim3 grid, int threads, size_t smem, int N, int S, int K2T, int NST,
-                             int NPL, const float *B32, const float2 *fin, float2 *Q,
-                             cudaStream_t st) {
+                             int NPL, int C, const float *B32, const float2 *fin, float2 *Q,
+                             float4 *partial, cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(calq32_kernel<TMA, MAXT, HLS>,
+    cudaError_t e = cudaFuncSetAttribute(calq32_kernel<TMA, MAXT, HLS, WS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(calq32)");
     configured = true;
   }
-  calq32_kernel<TMA, MAXT, HLS><<<grid, threads, smem, st>>>(N, S, K2T, NST, NPL, B32, fin, Q);
+  calq32_kernel<TMA, MAXT, HLS, WS>
+      <<<grid, threads, smem, st>>>(N, S, K2T, NST, NPL, C, B32, fin, Q, partial);
   EDB_LAUNCHED();
   return EDB_OK;
 }
 
 edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin, float2 *d_Q,
-                               cudaStream_t st, int variant) {
+                               cudaStream_t st, int variant, int C, float4 *d_partial) {
   if (variant < 0 || variant >= calq32_variants()) variant = 0;
+  if (C < 1 || C > N) return fail(EDB_EINVAL, "calq32: chunk count must be in [1, N]");
+  if (C > 1 && !d_partial) return fail(EDB_EINVAL, "calq32: chunks need a partial-sum buffer");
   const int maxt = variant_maxt(variant);
+  const int WS = variant_ws(variant);
+  const int SG = SC * WS;
   const bool hls = variant == 1;
   const int R = (N + A - 1) / A;
   int K2T = maxt / (R * WS);
@@ -734,29 +780,42 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   if (tma) {
     NST = 0;
     for (int ns = MAX_ST; ns >= 3 && !NST; --ns)
-      if (c32_geom(N, K2T, ns, 2, hlt).bytes <= cap) {
+      if (c32_geom(N, K2T, ns, 2, hlt, SG).bytes <= cap) {
         NST = ns;
         NPL = 2;
       }
     for (int ns = MAX_ST; ns >= 2 && !NST; --ns)
-      if (c32_geom(N, K2T, ns, 1, hlt).bytes <= cap) {
+      if (c32_geom(N, K2T, ns, 1, hlt, SG).bytes <= cap) {
         NST = ns;
         NPL = 1;
       }
     if (!NST) return fail(EDB_EINVAL, "calq32: this variant does not fit in shared memory");
   }
-  const C32Geom g = c32_geom(N, K2T, NST, NPL, hlt);
+  const C32Geom g = c32_geom(N, K2T, NST, NPL, hlt, SG);
   if (g.bytes > cap) return fail(EDB_EINVAL, "calq32: this variant does not fit in shared memory");
-  dim3 grid((unsigned)((S + SG - 1) / SG), (unsigned)N, (unsigned)tiles);
-  if (tma)
-    return hls ? launch_c32<true, 384, true>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
-                                             d_fin, d_Q, st)
-               : launch_c32<true, 256, false>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
-                                              d_fin, d_Q, st);
-  return hls ? launch_c32<false, 384, true>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
-                                            d_fin, d_Q, st)
-             : launch_c32<false, 256, false>(grid, threads, g.bytes, N, S, K2T, NST, NPL, d_B32,
-                                             d_fin, d_Q, st);
+  dim3 grid((unsigned)(((S + SG - 1) / SG) * C), (unsigned)N, (unsigned)tiles);
+  edb_status rc;
+  if (variant == 2)
+    rc = tma ? launch_c32<true, 256, false, 2>(grid, threads, g.bytes, N, S, K2T, NST, NPL, C,
+                                               d_B32, d_fin, d_Q, d_partial, st)
+             : launch_c32<false, 256, false, 2>(grid, threads, g.bytes, N, S, K2T, NST, NPL, C,
+                                                d_B32, d_fin, d_Q, d_partial, st);
+  else if (hls)
+    rc = tma ? launch_c32<true, 384, true, 8>(grid, threads, g.bytes, N, S, K2T, NST, NPL, C,
+                                              d_B32, d_fin, d_Q, d_partial, st)
+             : launch_c32<false, 384, true, 8>(grid, threads, g.bytes, N, S, K2T, NST, NPL, C,
+                                               d_B32, d_fin, d_Q, d_partial, st);
+  else
+    rc = tma ? launch_c32<true, 256, false, 8>(grid, threads, g.bytes, N, S, K2T, NST, NPL, C,
+                                               d_B32, d_fin, d_Q, d_partial, st)
+             : launch_c32<false, 256, false, 8>(grid, threads, g.bytes, N, S, K2T, NST, NPL, C,
+                                                d_B32, d_fin, d_Q, d_partial, st);
+  if (rc != EDB_OK || C == 1) return rc;
+  const long long n = (long long)S * N * N * N;
+  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+  calq32_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(n, C, d_partial, d_Q);
+  EDB_LAUNCHED();
+  return EDB_OK;
 }
 
 edb_status read_calq32_status(int *status, bool clear) {

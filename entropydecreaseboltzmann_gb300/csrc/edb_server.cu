@@ -18,9 +18,12 @@
 //                 mostly empty); their initial data is uploaded and
 //                 transformed in chunks;
 //   step          one replay of the group's captured CUDA graph for the
-//                 bucket S = live rounded up to 16 (the batched kernel's
-//                 solve group) advances every live solve by one step; padding
-//                 slots hold zero solves.
+//                 bucket S = live rounded up to 4 (the batched kernel's
+//                 smallest solve group) advances every live solve by one
+//                 step; padding slots hold zero solves.  Q-hat runs chunked
+//                 over the l1 planes (a chunk count fixed per N), so a few
+//                 live solves still fill the GPU and a result does not depend
+//                 on the bucket it ran in.
 // Groups run concurrently on their own streams.  Each solve's arithmetic
 // depends only on its own slot, so a result is the same alone and in a mix.
 #include <math.h>
@@ -40,7 +43,7 @@
 namespace edb {
 namespace {
 
-constexpr int BUCKET = 16;  // graph bucket granularity (solves)
+constexpr int BUCKET = 4;   // graph bucket granularity (solves)
 constexpr int XFER = 64;    // solves per admission / retirement transfer chunk
 
 using Clock = std::chrono::steady_clock;
@@ -68,6 +71,8 @@ struct Group {
   float2 *Qs[4] = {nullptr, nullptr, nullptr, nullptr}, *in32 = nullptr;
   EfixState *state = nullptr;
   double *m0 = nullptr, *H = nullptr;
+  float4 *part = nullptr;  // chunk partial sums of one Q-hat stage
+  int C = 1;               // l1-plane chunks of the batched kernel
   // fixed per group
   double *ctab = nullptr, *trd = nullptr, *xin = nullptr;
   double2 *xo = nullptr, *xF = nullptr;
@@ -119,10 +124,16 @@ double now_s(const edb_server *s) {
   return std::chrono::duration<double>(Clock::now() - s->t0).count();
 }
 
-long long slot_bytes(const edb_server *s, long long NQ) {
-  // Fhat, F (complex FP64), stage arrays, FP32 Q-hat stages, FP32 input copy
+// Chunk count of the batched kernel for a table of N (fixed per N).
+int chunks_of(int N) { return N < 8 ? N : 8; }
+
+long long slot_bytes(const edb_server *s, int N) {
+  // Fhat, F (complex FP64), stage arrays, FP32 Q-hat stages, FP32 input copy,
+  // chunk partial sums
+  const long long NQ = (long long)N * N * N;
   const int nst = s->nstage > 0 ? s->nstage : ((s->d.conserve && s->d.fix_entropy) ? 1 : 0);
-  return NQ * (16 + 16 + 16LL * nst + 8LL * s->nq + 8) + (long long)sizeof(EfixState) + 48;
+  return NQ * (16 + 16 + 16LL * nst + 8LL * s->nq + 8 + 16LL * chunks_of(N)) +
+         (long long)sizeof(EfixState) + 48;
 }
 
 long long table_bytes_of(int N) {
@@ -149,6 +160,7 @@ void free_arena(Group &g) {
   dfree(g.state);
   dfree(g.m0);
   dfree(g.H);
+  dfree(g.part);
 }
 
 void drop_graphs(Group &g) {
@@ -188,6 +200,7 @@ edb_status get_group(edb_server *s, int N, double gamma, double R, int *out) {
   g->gamma = gamma;
   g->R = R;
   g->NQ = (long long)N * N * N;
+  g->C = chunks_of(N);
   const size_t NQ = (size_t)g->NQ;
   edb_qcalc_desc qd;
   qd.N = N;
@@ -235,7 +248,7 @@ edb_status get_group(edb_server *s, int N, double gamma, double R, int *out) {
 // Resizes the arena to newcap slots, keeping the live prefix.
 edb_status resize_arena(edb_server *s, Group &g, int newcap) {
   if (g.st) EDB_CUDA(cudaStreamSynchronize(g.st));
-  const long long nb = (long long)newcap * slot_bytes(s, g.NQ);
+  const long long nb = (long long)newcap * slot_bytes(s, g.N);
   if (s->bytes_used - g.arena_bytes + nb > (long long)s->d.hbm_budget_bytes)
     return fail(EDB_ENOMEM, "HBM budget");
   Group ng;  // new arrays only
@@ -249,6 +262,7 @@ edb_status resize_arena(edb_server *s, Group &g, int newcap) {
   if (rc == EDB_OK) rc = dalloc(&ng.state, (size_t)newcap);
   if (rc == EDB_OK) rc = dalloc(&ng.m0, (size_t)newcap * 5);
   if (rc == EDB_OK) rc = dalloc(&ng.H, (size_t)newcap);
+  if (rc == EDB_OK && g.C > 1) rc = dalloc(&ng.part, n * (size_t)g.C);
   if (rc != EDB_OK) {
     free_arena(ng);
     return rc;
@@ -287,6 +301,7 @@ edb_status resize_arena(edb_server *s, Group &g, int newcap) {
   g.state = ng.state;
   g.m0 = ng.m0;
   g.H = ng.H;
+  g.part = ng.part;
   ng = Group();
   account(s, nb - g.arena_bytes);
   g.arena_bytes = nb;
@@ -303,8 +318,10 @@ edb_status record_step(edb_server *s, Group &g, int S, cudaStream_t st) {
   const float *B32 = qcalc_B32(g.q);
   double2 *Fh = g.Fhat, **F = g.Fs;
   float2 **Q = g.Qs, *in = g.in32;
-  const int variant = qcalc_c32_variant(g.q, S, nullptr);
-  auto calq = [&](float2 *out) { return launch_calq32_batch(N, S, B32, in, out, st, variant); };
+  const int variant = qcalc_c32_variant(g.q, S, nullptr, g.C > 1);
+  auto calq = [&](float2 *out) {
+    return launch_calq32_batch(N, S, B32, in, out, st, variant, g.C, g.part);
+  };
   switch (s->d.scheme) {
     case EDB_SCHEME_FE:
       EDB_TRY(calq(Q[0]));
@@ -359,10 +376,9 @@ edb_status step_graph(edb_server *s, Group &g, int S, cudaGraphExec_t *exec, int
     return EDB_OK;
   }
   bool tuned = false;
-  qcalc_c32_variant(g.q, S, &tuned);
+  qcalc_c32_variant(g.q, S, &tuned, g.C > 1);
   if (!tuned)  // before capture: the graph bakes the variant in
-    EDB_TRY(edb_qcalc_autotune_batch(g.q, S, (const float *)g.in32, (float *)g.Qs[0], g.st,
-                                     nullptr));
+    EDB_TRY(qcalc_autotune_split(g.q, S, g.in32, g.Qs[0], g.st, g.C, g.part));
   const long long before = edb_kernel_launch_count();
   cudaGraph_t graph = nullptr;
   EDB_CUDA(cudaStreamBeginCapture(g.st, cudaStreamCaptureModeThreadLocal));
@@ -410,7 +426,7 @@ edb_status admit(edb_server *s, Group &g, int gi) {
       int want = std::max(g.cap * 2, ((g.live + k + BUCKET - 1) / BUCKET) * BUCKET);
       if (s->d.max_live_per_group > 0)
         want = std::min(want, ((limit + BUCKET - 1) / BUCKET) * BUCKET);
-      const long long sb = slot_bytes(s, g.NQ);
+      const long long sb = slot_bytes(s, g.N);
       auto fit = [&]() {  // largest capacity (whole buckets) the budget allows
         const long long avail = (long long)s->d.hbm_budget_bytes - (s->bytes_used - g.arena_bytes);
         return (int)(avail / sb) / BUCKET * BUCKET;
@@ -610,7 +626,7 @@ extern "C" edb_status edb_server_submit(edb_server *s, const edb_request *r, con
   if (!(r->gamma >= 0 && r->gamma <= 2)) return fail(EDB_EINVAL, "gamma must be in [0, 2]");
   if (r->steps < 1) return fail(EDB_EINVAL, "steps must be >= 1");
   const long long NQ = (long long)r->N * r->N * r->N;
-  if (table_bytes_of(r->N) + fixed_bytes_of(r->N) + BUCKET * slot_bytes(s, NQ) >
+  if (table_bytes_of(r->N) + fixed_bytes_of(r->N) + BUCKET * slot_bytes(s, r->N) >
       (long long)s->d.hbm_budget_bytes)
     return fail(EDB_ENOMEM, "request cannot fit the HBM budget");
   Req q;
@@ -710,6 +726,12 @@ extern "C" edb_status edb_server_result(edb_server *s, long long id, double *F_r
   if (!r.r.want_result) return fail(EDB_ENOTFOUND, "result not kept (want_result = 0)");
   if (F_real) memcpy(F_real, r.F.data(), sizeof(double) * r.F.size());
   if (Fhat) memcpy(Fhat, r.Fhat.data(), sizeof(double) * r.Fhat.size());
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_server_clock(edb_server *s, double *t) {
+  if (!s || !t) return fail(EDB_EINVAL, "null argument");
+  *t = now_s(s);
   return EDB_OK;
 }
 

@@ -133,6 +133,18 @@ edb_status edb_qcalc_calQ_device(edb_qcalc *q, const double *d_fin, double *d_Qo
 edb_status edb_qcalc_calQ_batch_f32_device(edb_qcalc *q, int S, const float *d_fin,
                                            float *d_Qout, void *stream);
 
+/* The batched kernel with an explicit variant and chunk count (no reference
+ * counterpart; the autotuner and the serving engine choose these).
+ * variant 0/1: 16-solve groups (CTA <= 256 threads with the compensated sums
+ * in registers / <= 384 threads with them in shared memory); variant 2:
+ * 4-solve groups.  chunks > 1 splits the l1 planes into that many chunks
+ * whose compensated sums are added in order in FP64; d_partial (device)
+ * then holds chunks x S x N^3 x 16 bytes.  For a given chunk count the result
+ * of each solve does not depend on S or the variant. */
+edb_status edb_qcalc_calQ_batch_f32_ex(edb_qcalc *q, int S, int variant, int chunks,
+                                       void *d_partial, const float *d_fin, float *d_Qout,
+                                       void *stream);
+
 /* FP64 collision sum that allocates nothing, for callers that may not call
  * cudaMalloc (a host that owns a fixed device pool and accounts for every
  * byte, a plugin inside such a host, a real-time loop that cannot take
@@ -349,6 +361,8 @@ edb_status edb_server_run(edb_server *s, double max_wall_s);
 edb_status edb_server_result(edb_server *s, long long id, double *F_real, double *Fhat,
                              edb_request_info *info);
 edb_status edb_server_get_stats(edb_server *s, edb_server_stats *out);
+/* The server clock (seconds since the first edb_server_run; 0 before). */
+edb_status edb_server_clock(edb_server *s, double *t);
 
 /* -------------------------------------------------------- conservation */
 /* No reference counterpart: the moment functionals of conservative mode.

@@ -198,6 +198,41 @@ def test_batch_result_same_alone_and_in_the_mix(edb):
         assert torch.equal(one[0], mix[s])
 
 
+@pytest.mark.parametrize("N,L,chunks", [(8, 6.0, 4), (16, 6.0, 8), (24, 7.0, 8)])
+def test_calQ_batch_variants_and_chunks(edb, oracle, N, L, chunks):
+    """Every variant (16- and 4-solve groups, registers / shared memory for
+    the compensated sums) gives bit-identical results for a given chunk count,
+    a solve alone equals the same solve in a batch, and chunked and unchunked
+    results meet the FP32 tolerance (relative L2 <= 5e-6) against the FP64
+    oracle."""
+    import torch
+
+    S = 11
+    _, fh = _batch_inputs(N, L, S, seed=40 + N)
+    q = edb.QCalculator(N, 0, L=L, filter=False, index_mode=INDEX_ALIASED)
+    q.genB()
+    fin = torch.from_numpy(fh.astype(np.complex64)).cuda()
+    part = torch.empty(chunks * S * N ** 3 * 4, dtype=torch.float32, device="cuda")
+    res = {}
+    for C in (1, chunks):
+        for v in (0, 1, 2):
+            out = torch.empty_like(fin)
+            q.calQ_batch_f32_ex(S, v, C, part, fin, out)
+            torch.cuda.synchronize()
+            res[(C, v)] = out.cpu().numpy()
+        assert np.array_equal(res[(C, 0)], res[(C, 1)]) and np.array_equal(res[(C, 0)], res[(C, 2)])
+        one = torch.empty_like(fin[3:4])
+        q.calQ_batch_f32_ex(1, 2, C, part, fin[3:4].contiguous(), one)
+        torch.cuda.synchronize()
+        assert np.array_equal(one.cpu().numpy()[0], res[(C, 0)][3])
+    Bo = oracle.genB(N, 0.0, L, False, INDEX_ALIASED)
+    for s in (0, 7):
+        Qo = oracle.calQ(N, Bo, fh[s], INDEX_ALIASED)
+        for C in (1, chunks):
+            assert rel_l2(res[(C, 0)][s], Qo) <= 5e-6
+    assert edb.device_status() == 0
+
+
 def test_device_calQ_matches_host_calQ(edb):
     import torch
 

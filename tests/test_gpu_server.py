@@ -118,8 +118,8 @@ def test_continuous_admission_and_budget(edb):
     assert st["completed"] == 2 and st["tts_p50_s"] <= st["tts_p99_s"]
     srv.close()
     # a budget of one table (N^6 x 4 B = 11.9 MB), its transfer staging
-    # (64 x N^3 x 40 B = 4.4 MB) and about 36 slots (N^3 x 120 B each, RK4),
-    # so the 70 requests are served in waves of whole 16-solve buckets
+    # (64 x N^3 x 40 B = 4.4 MB) and about 17 slots (N^3 x 248 B each: RK4
+    # stages plus 8 chunk partial sums), so the 70 requests are served in waves
     srv = edb.Server(hbm_budget_bytes=2.4e7, scheme=edb.SCHEME_RK4, dt=0.01)
     for j in range(70):
         srv.submit(N, 0.0, R, 3, f)
@@ -156,3 +156,20 @@ def test_conservative_serving(edb):
         m, m0 = phi @ F * h ** 3, phi @ f0[i] * h ** 3
         sc = np.array([m0[0], *(3 * [np.sqrt(m0[0] * m0[4])]), m0[4]])
         assert np.max(np.abs(m - m0) / sc) <= 1e-10
+
+
+def test_uneven_batch_small(edb):
+    """The uneven-batch workload at reduced size: 4 solves per N in
+    {16, 24, 32} with gamma drawn from {0, 0.5, 1} (up to 9 tables, the
+    non-integer gamma through quadrature), SSP3 with the moment-preserving
+    fix, 3-8 steps each; every request completes."""
+    from entropydecreaseboltzmann_gb300 import serving
+
+    reqs = serving.uneven_requests(4, seed=7, steps=(3, 8))
+    srv = edb.Server(hbm_budget_bytes=40e9, scheme=edb.SCHEME_SSP3, dt=0.005, fix_entropy=True,
+                     conserve=True)
+    st, _ = serving.run(srv, reqs, 0.005)
+    assert st["completed"] == len(reqs) == 12
+    assert 3 <= st["groups"] <= 9
+    assert edb.device_status() == 0
+    srv.close()
