@@ -138,6 +138,8 @@ def _load():
         "edb_batch_moments": (C.c_int, [_vp, _dp, _dp]),
         "edb_batch_launches_per_step": (C.c_int, [_vp, _ip]),
         "edb_qcalc_genB_f32": (C.c_int, [_vp]),
+        "edb_funF": (C.c_int, [C.c_int, C.c_longlong, _dp, _dp, _dp]),
+        "edb_filtering": (C.c_int, [C.c_int, C.c_longlong, _ip, _dp]),
         "edb_server_create": (C.c_int, [C.POINTER(ServerDesc), C.POINTER(_vp)]),
         "edb_server_destroy": (C.c_int, [_vp]),
         "edb_server_prepare": (C.c_int, [_vp, C.c_int, C.c_double, C.c_double]),

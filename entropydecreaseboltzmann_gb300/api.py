@@ -73,6 +73,23 @@ class QCalculator:
     def genB(self):
         check(lib.edb_qcalc_genB(self._h))
 
+    def funF(self, xi, eta):
+        """funF(xi, eta) (QCalculator.h:76-106) for this calculator's alpha,
+        evaluated on the device; scalars or arrays."""
+        x = np.ascontiguousarray(np.atleast_1d(xi), dtype=np.float64)
+        e = np.ascontiguousarray(np.broadcast_to(np.atleast_1d(eta), x.shape), dtype=np.float64)
+        out = np.empty_like(x)
+        check(lib.edb_funF(int(round(self.desc.gamma)) if float(self.desc.gamma).is_integer()
+                           else -1, x.size, dptr(x), dptr(e), dptr(out)))
+        return float(out[0]) if np.ndim(xi) == 0 else out
+
+    def filtering(self, beta):
+        """filtering(beta) (QCalculator.h:67-74), evaluated on the device."""
+        b = np.ascontiguousarray(np.atleast_1d(beta), dtype=np.int32)
+        out = np.empty(b.shape, dtype=np.float64)
+        check(lib.edb_filtering(self.N, b.size, b.ctypes.data_as(C.POINTER(C.c_int)), dptr(out)))
+        return float(out[0]) if np.ndim(beta) == 0 else out
+
     def calQ(self, Qout, fin):
         """calQ(Qout, fin) (QCalculator.h:231-257): Qout <- Q-hat(fin), FP64."""
         fin = _c128(fin, self.NQ)

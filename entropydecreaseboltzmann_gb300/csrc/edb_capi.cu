@@ -256,6 +256,46 @@ extern "C" edb_status edb_qcalc_genB(edb_qcalc *q) {
   return qcalc_tune_fp64(q);
 }
 
+extern "C" edb_status edb_funF(int alpha, long long n, const double *xi, const double *eta,
+                               double *out) {
+  if (n < 0 || (n > 0 && (!xi || !eta || !out))) return fail(EDB_EINVAL, "bad argument");
+  if (n == 0) return EDB_OK;
+  EDB_TRY(ensure_device());
+  double *d = nullptr;
+  EDB_TRY(dalloc(&d, (size_t)n * 3));
+  cudaError_t e = cudaMemcpy(d, xi, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + n, eta, sizeof(double) * n, cudaMemcpyHostToDevice);
+  edb_status rc = e == cudaSuccess ? launch_funF_points(alpha, n, d, d + n, d + 2 * n, nullptr)
+                                   : cuda_fail(e, "funF upload");
+  if (rc == EDB_OK) {
+    e = cudaMemcpy(out, d + 2 * n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = cuda_fail(e, "funF download");
+  }
+  dfree(d);
+  return rc;
+}
+
+extern "C" edb_status edb_filtering(int N, long long n, const int *beta, double *out) {
+  if (N < 3 || N > 64 || n < 0 || (n > 0 && (!beta || !out))) return fail(EDB_EINVAL, "bad argument");
+  if (n == 0) return EDB_OK;
+  EDB_TRY(ensure_device());
+  int *db = nullptr;
+  double *dout = nullptr;
+  EDB_TRY(dalloc(&db, (size_t)n));
+  edb_status rc = dalloc(&dout, (size_t)n);
+  cudaError_t e = cudaSuccess;
+  if (rc == EDB_OK) e = cudaMemcpy(db, beta, sizeof(int) * n, cudaMemcpyHostToDevice);
+  if (rc == EDB_OK && e != cudaSuccess) rc = cuda_fail(e, "filtering upload");
+  if (rc == EDB_OK) rc = launch_filtering_points(N, n, db, dout, nullptr);
+  if (rc == EDB_OK) {
+    e = cudaMemcpy(out, dout, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = cuda_fail(e, "filtering download");
+  }
+  dfree(db);
+  dfree(dout);
+  return rc;
+}
+
 extern "C" edb_status edb_qcalc_genB_f32(edb_qcalc *q) {
   if (!q) return fail(EDB_EINVAL, "null handle");
   if (q->d.index_mode != EDB_INDEX_ALIASED)

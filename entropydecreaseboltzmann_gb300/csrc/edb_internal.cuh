@@ -85,6 +85,13 @@ edb_status launch_genB(int N, double gamma, double L, int filter, int mode, cons
                        int amax, const double *d_sigma, const double *d_Bmm, double *d_B64,
                        float *d_B32, cudaStream_t st);
 
+// QCalculator::funF (alpha 0/1 closed forms, other alpha -> 0) and
+// ::filtering at n points.
+edb_status launch_funF_points(int alpha, long long n, const double *d_xi, const double *d_eta,
+                              double *d_out, cudaStream_t st);
+edb_status launch_filtering_points(int N, long long n, const int *d_beta, double *d_out,
+                                   cudaStream_t st);
+
 // FP64 calQ: partial sums over l-chunks then an ordered reduction + output
 // conversion.  d_partial holds nchunk * KC complex doubles.
 int calq64_nchunk(const QParams &p);

@@ -268,4 +268,36 @@ edb_status launch_genB(int N, double gamma, double L, int filter, int mode, cons
   return EDB_OK;
 }
 
+// ---- pointwise evaluation (QCalculator::funF, ::filtering as public methods)
+__global__ void funF_points_kernel(int alpha, long long n, const double *__restrict__ xi,
+                                   const double *__restrict__ eta, double *__restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = funF_closed(alpha, xi[i], eta[i]);
+}
+
+__global__ void filtering_points_kernel(int N, double PI, long long n, const int *__restrict__ beta,
+                                        double *__restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int nn = (N - 1) / 2;
+  const double tmp = (double)(nn + 1);
+  const double b = fabs((double)beta[i]);
+  out[i] = ((tmp - b) * cos(PI * b / tmp) + sin(PI * b / tmp) / tan(PI / tmp)) / tmp;
+}
+
+edb_status launch_funF_points(int alpha, long long n, const double *d_xi, const double *d_eta,
+                              double *d_out, cudaStream_t st) {
+  funF_points_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(alpha, n, d_xi, d_eta, d_out);
+  EDB_LAUNCHED();
+  return EDB_OK;
+}
+
+edb_status launch_filtering_points(int N, long long n, const int *d_beta, double *d_out,
+                                   cudaStream_t st) {
+  const double PI = 4. * atan(1.);
+  filtering_points_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(N, PI, n, d_beta, d_out);
+  EDB_LAUNCHED();
+  return EDB_OK;
+}
+
 }  // namespace edb

@@ -113,6 +113,14 @@ edb_status edb_qcalc_close_filter(edb_qcalc *q);
  * F_gamma = int_0^1 r^(2+gamma) sinc(xi r) sinc(eta r) dr (ReadMe.md:51). */
 edb_status edb_qcalc_genB(edb_qcalc *q);
 
+/* QCalculator::funF(xi, eta) (QCalculator.h:76-106) at n points, evaluated
+ * on the device: the closed forms for alpha 0 and 1, 0 for any other alpha
+ * (as the reference).  Host arrays, synchronous. */
+edb_status edb_funF(int alpha, long long n, const double *xi, const double *eta, double *out);
+/* QCalculator::filtering(beta) (QCalculator.h:67-74) of an N-mode
+ * calculator at n integer points, on the device.  Host arrays. */
+edb_status edb_filtering(int N, long long n, const int *beta, double *out);
+
 /* genB for batched use only (ALIASED mode): builds just the FP32 FFTW-order
  * table (4 bytes per entry instead of 8 + 8 + 4), so many tables fit in one
  * HBM budget.  The FP64 calQ entry points then report EDB_ENOTREADY. */

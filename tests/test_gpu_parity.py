@@ -294,3 +294,22 @@ def test_fp64_emulated_kernel_matches_native_and_oracle(edb, oracle, N, mode):
         assert rel_l2(Qe, Qn) <= 1e-12
         if Bo is not None:
             assert rel_l2(Qe, oracle.calQ(N, Bo, fin, mode)) <= 1e-12
+
+
+def test_funF_and_filtering_on_device_match_reference_golden(edb, golden):
+    """QCalculator.funF / .filtering (device evaluation) against the
+    reference's values: <= 1e-13 of the largest value (CUDA's and glibc's
+    sin/cos differ in the last bits, which cancellation near xi = eta
+    magnifies relative to small values, as for genB)."""
+    grid, vals = golden["funF_grid"], golden["funF_val"]
+    for alpha in (0, 1):
+        sel = grid[:, 0] == alpha
+        q = edb.QCalculator(5, alpha)
+        got = q.funF(grid[sel, 1], grid[sel, 2])
+        want = vals[sel]
+        assert np.max(np.abs(got - want)) <= 1e-13 * np.max(np.abs(want))
+    for N in sorted(set(int(n) for n in golden["filtering"][:, 0])):
+        rows = golden["filtering"][golden["filtering"][:, 0] == N]
+        q = edb.QCalculator(N, 0)
+        got = q.filtering(rows[:, 1].astype(np.int32))
+        assert np.max(np.abs(got - rows[:, 2])) <= 1e-13 * np.max(np.abs(rows[:, 2]))
