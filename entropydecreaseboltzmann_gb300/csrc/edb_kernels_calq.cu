@@ -158,7 +158,7 @@ edb_status launch_calq64_reduce(const QParams &p, int nchunk, const double2 *d_p
 //
 // CTA = (group of SG = 2 WS solves) x (one k1, a tile of K2T k2 values, all
 // k3) x (a chunk of l1 planes).  Thread = (solve pair {w, w+WS}, k2, run of
-// A = 8 consecutive k3).  WS = 8 (16-solve groups) for throughput; WS = 2
+// A = 8 or 4 consecutive k3).  WS = 8 (16-solve groups) for throughput; WS = 2
 // (4-solve groups) for the few live solves of a serving table.  The CTA walks
 // the l-lines (l1, l2) of its chunk in order; for each line it needs
 //   B[(l1,l2,l3)][k1, k2-tile, all k3]  N rows of K2T*N floats (the B tile),
@@ -193,7 +193,6 @@ edb_status launch_calq64_reduce(const QParams &p, int nchunk, const double2 *d_p
 // result does not depend on what else is in the batch.
 // ---------------------------------------------------------------------------
 namespace {
-constexpr int A = 8;                      // k3 outputs per thread
 constexpr int SC = 2;                     // solves per thread: w and w + WS
 constexpr int ROWPAD = 8;                 // floats after each B-tile row
 constexpr int FLPAD = 2;                  // complex after each f_l line
@@ -206,7 +205,7 @@ __device__ int g_calq32_status;  // nonzero: a bounded wait ran out
 constexpr int MAX_ST = 4;                 // pipeline stages (l-lines in flight)
 
 struct C32Geom {
-  int N, R, RA, K2T, BROW, FLS, PSTR, NST, NPL, HLT, SG;
+  int N, A, R, RA, K2T, BROW, FLS, PSTR, NST, NPL, HLT, SG;
   size_t off_B, off_fl, off_pl, off_hl, bytes;
 };
 
@@ -214,9 +213,11 @@ struct C32Geom {
 // m1-planes and, when HLT > 0, the compensated (hi, lo) sums of HLT threads
 // (2 * A * SC packed pairs each, thread-fastest so accesses never conflict).
 // Barriers: full[MAX_ST], empty[MAX_ST], plane[2].
-__host__ __device__ inline C32Geom c32_geom(int N, int K2T, int NST, int NPL, int HLT, int SG) {
+__host__ __device__ inline C32Geom c32_geom(int N, int A, int K2T, int NST, int NPL, int HLT,
+                                            int SG) {
   C32Geom g;
   g.SG = SG;
+  g.A = A;
   g.N = N;
   g.R = (N + A - 1) / A;
   g.RA = g.R * A;
@@ -344,13 +345,6 @@ __device__ __forceinline__ void two_sum_fold2(u64 &hi, u64 &lo, u64 x) {
   lo = add2(lo, e);
 }
 
-__device__ __forceinline__ void two_sum_fold(float &hi, float &lo, float x) {
-  float s = hi + x;
-  float bb = s - hi;
-  float e = (hi - (s - bb)) + (x - bb);
-  hi = s;
-  lo += e;
-}
 
 // Issue (TMA: warp 0, one copy per lane) or perform (plain: all threads) the
 // staging of the B tile and f_l line of line li into buffer `st`.
@@ -411,8 +405,9 @@ __device__ __forceinline__ void stage_plane(const C32Geom &g, int m1, int s0, in
 // One l-line for this thread: A outputs x SC solves.  BIGN: N >= A, so one
 // conditional add brings a ring index back into [0, N).  VEC: N % 4 == 0, so
 // every B-tile row offset is 16-byte aligned and B is read with float4 loads;
-// otherwise with scalar loads.
-template <bool BIGN, bool VEC>
+// otherwise with scalar loads.  Each output's sum runs over l3 in order
+// whatever A is, so every A gives the same bits.
+template <bool BIGN, bool VEC, int A>
 __device__ __forceinline__ void compute_line(const C32Geom &g, const float *Bt, const float2 *fl0,
                                              const float2 *fl1, const float2 *p0,
                                              const float2 *p1, int k3_0, u64 (&accA)[A][SC],
@@ -453,10 +448,14 @@ __device__ __forceinline__ void compute_line(const C32Geom &g, const float *Bt, 
       }
       float bv[A];
       if (VEC) {
-        const float4 b0 = *reinterpret_cast<const float4 *>(Bt + (size_t)l3 * g.BROW);
-        const float4 b1 = *reinterpret_cast<const float4 *>(Bt + (size_t)l3 * g.BROW + 4);
-        bv[0] = b0.x; bv[1] = b0.y; bv[2] = b0.z; bv[3] = b0.w;
-        bv[4] = b1.x; bv[5] = b1.y; bv[6] = b1.z; bv[7] = b1.w;
+#pragma unroll
+        for (int q4 = 0; q4 < A / 4; ++q4) {
+          const float4 b = *reinterpret_cast<const float4 *>(Bt + (size_t)l3 * g.BROW + 4 * q4);
+          bv[4 * q4] = b.x;
+          bv[4 * q4 + 1] = b.y;
+          bv[4 * q4 + 2] = b.z;
+          bv[4 * q4 + 3] = b.w;
+        }
       } else {
 #pragma unroll
         for (int a = 0; a < A; ++a) bv[a] = Bt[(size_t)l3 * g.BROW + a];
@@ -486,14 +485,14 @@ __device__ __forceinline__ void compute_line(const C32Geom &g, const float *Bt, 
 // instead of registers, which frees 64 registers per thread for more resident
 // warps.  WS: solve lanes (group of 2 WS solves).  The autotuner picks the
 // variant per (table, S).
-template <bool TMA, int MAXT, bool HLS, int WS>
-__global__ void __launch_bounds__(MAXT, 1)
+template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
     calq32_kernel(int N, int S, int K2T, int NST, int NPL, int C, const float *__restrict__ B32,
                   const float2 *__restrict__ fin, float2 *__restrict__ Q,
                   float4 *__restrict__ partial) {
   constexpr int SG = SC * WS;
   extern __shared__ __align__(128) unsigned char smem[];
-  const C32Geom g = c32_geom(N, K2T, NST, NPL, HLS ? (int)blockDim.x : 0, SG);
+  const C32Geom g = c32_geom(N, A, K2T, NST, NPL, HLS ? (int)blockDim.x : 0, SG);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);  // [MAX_ST]
   uint64_t *empty = full + MAX_ST;                       // [MAX_ST]
   uint64_t *pbar = full + 2 * MAX_ST;                    // [2] planes
@@ -627,9 +626,9 @@ __global__ void __launch_bounds__(MAXT, 1)
     const float2 *p0 = plb + (size_t)pb * plane_sz + (size_t)w * g.PSTR + m2 * N;
     const float2 *p1 = p0 + (size_t)WS * g.PSTR;
     if (TMA)
-      compute_line<true, true>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
+      compute_line<true, true, A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
     else
-      compute_line<false, false>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
+      compute_line<false, false, A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
     if (TMA) {
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[st]);
@@ -725,31 +724,64 @@ __global__ void calq32_reduce_kernel(long long n, int C, const float4 *__restric
   }
 }
 
-// Variants the autotuner chooses from:
-//   0: 16-solve groups, CTA <= 256 threads, (hi, lo) in registers (<= 255 registers)
-//   1: 16-solve groups, CTA <= 384 threads, (hi, lo) in shared memory (168 registers)
-//   2: 4-solve groups, CTA <= 256 threads, (hi, lo) in registers
-int calq32_variants() { return 3; }
+// Variants the autotuner chooses from (solve lanes WS, k3 outputs per
+// thread A, CTA-size bound, where the compensated sums live, CTAs per SM the
+// register budget must allow):
+//   0: WS 8, A 8, <= 256 threads, registers (<= 255 registers)
+//   1: WS 8, A 8, <= 384 threads, shared memory (<= 168 registers)
+//   2: WS 2, A 8, <= 256 threads, registers        (4-solve groups)
+//   3: WS 8, A 4, <= 256 threads, registers, 2 CTAs per SM (<= 128 registers)
+//   4: WS 8, A 4, <= 384 threads, registers (<= 168 registers)
+struct C32Variant {
+  int ws, a, maxt;
+  bool hls;
+  int minb;
+};
+constexpr C32Variant kC32Variants[] = {
+    {8, 8, 256, false, 1}, {8, 8, 384, true, 1}, {2, 8, 256, false, 1},
+    {8, 4, 256, false, 2}, {8, 4, 384, false, 1}};
+int calq32_variants() { return (int)(sizeof(kC32Variants) / sizeof(kC32Variants[0])); }
+int calq32_group(int variant) { return SC * kC32Variants[variant].ws; }
 
-static int variant_maxt(int v) { return v == 1 ? 384 : 256; }
-static int variant_ws(int v) { return v == 2 ? 2 : 8; }
-int calq32_group(int variant) { return SC * variant_ws(variant); }
-
-template <bool TMA, int MAXT, bool HLS, int WS>
+template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB>
 static edb_status launch_c32(dim3 grid, int threads, size_t smem, int N, int S, int K2T, int NST,
                              int NPL, int C, const float *B32, const float2 *fin, float2 *Q,
                              float4 *partial, cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(calq32_kernel<TMA, MAXT, HLS, WS>,
+    cudaError_t e = cudaFuncSetAttribute(calq32_kernel<TMA, MAXT, HLS, WS, A, MINB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(calq32)");
     configured = true;
   }
-  calq32_kernel<TMA, MAXT, HLS, WS>
+  calq32_kernel<TMA, MAXT, HLS, WS, A, MINB>
       <<<grid, threads, smem, st>>>(N, S, K2T, NST, NPL, C, B32, fin, Q, partial);
   EDB_LAUNCHED();
   return EDB_OK;
+}
+
+template <bool TMA>
+static edb_status launch_c32_variant(int v, dim3 grid, int threads, size_t smem, int N, int S,
+                                     int K2T, int NST, int NPL, int C, const float *B32,
+                                     const float2 *fin, float2 *Q, float4 *partial,
+                                     cudaStream_t st) {
+  switch (v) {
+    case 1:
+      return launch_c32<TMA, 384, true, 8, 8, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C, B32,
+                                                 fin, Q, partial, st);
+    case 2:
+      return launch_c32<TMA, 256, false, 2, 8, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C,
+                                                  B32, fin, Q, partial, st);
+    case 3:
+      return launch_c32<TMA, 256, false, 8, 4, 2>(grid, threads, smem, N, S, K2T, NST, NPL, C,
+                                                  B32, fin, Q, partial, st);
+    case 4:
+      return launch_c32<TMA, 384, false, 8, 4, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C,
+                                                  B32, fin, Q, partial, st);
+    default:
+      return launch_c32<TMA, 256, false, 8, 8, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C,
+                                                  B32, fin, Q, partial, st);
+  }
 }
 
 edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin, float2 *d_Q,
@@ -757,10 +789,9 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   if (variant < 0 || variant >= calq32_variants()) variant = 0;
   if (C < 1 || C > N) return fail(EDB_EINVAL, "calq32: chunk count must be in [1, N]");
   if (C > 1 && !d_partial) return fail(EDB_EINVAL, "calq32: chunks need a partial-sum buffer");
-  const int maxt = variant_maxt(variant);
-  const int WS = variant_ws(variant);
+  const C32Variant &vr = kC32Variants[variant];
+  const int maxt = vr.maxt, WS = vr.ws, A = vr.a;
   const int SG = SC * WS;
-  const bool hls = variant == 1;
   const int R = (N + A - 1) / A;
   int K2T = maxt / (R * WS);
   if (K2T > N) K2T = N;
@@ -768,48 +799,37 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   const int tiles = (N + K2T - 1) / K2T;
   K2T = (N + tiles - 1) / tiles;
   const int threads = K2T * R * WS;
-  const int hlt = hls ? threads : 0;
+  const int hlt = vr.hls ? threads : 0;
   // TMA bulk copies need 16-byte aligned sources: N % 4 == 0 makes every
   // row/line/plane offset a multiple of 16 bytes; the base pointers are checked
   const bool tma = (N % 4) == 0 && N >= A && ((uintptr_t)d_B32 % 16) == 0 &&
                    ((uintptr_t)d_fin % 16) == 0;
   // deepest pipeline that fits: two planes with >= 3 stages if possible,
   // else one plane with up to MAX_ST stages (the plain path uses 1 + 1)
-  const size_t cap = 227 * 1024;
+  const size_t cap = vr.minb == 2 ? 113 * 1024 : 227 * 1024;
   int NST = 1, NPL = 1;
   if (tma) {
     NST = 0;
     for (int ns = MAX_ST; ns >= 3 && !NST; --ns)
-      if (c32_geom(N, K2T, ns, 2, hlt, SG).bytes <= cap) {
+      if (c32_geom(N, A, K2T, ns, 2, hlt, SG).bytes <= cap) {
         NST = ns;
         NPL = 2;
       }
     for (int ns = MAX_ST; ns >= 2 && !NST; --ns)
-      if (c32_geom(N, K2T, ns, 1, hlt, SG).bytes <= cap) {
+      if (c32_geom(N, A, K2T, ns, 1, hlt, SG).bytes <= cap) {
         NST = ns;
         NPL = 1;
       }
     if (!NST) return fail(EDB_EINVAL, "calq32: this variant does not fit in shared memory");
   }
-  const C32Geom g = c32_geom(N, K2T, NST, NPL, hlt, SG);
+  const C32Geom g = c32_geom(N, A, K2T, NST, NPL, hlt, SG);
   if (g.bytes > cap) return fail(EDB_EINVAL, "calq32: this variant does not fit in shared memory");
   dim3 grid((unsigned)(((S + SG - 1) / SG) * C), (unsigned)N, (unsigned)tiles);
-  edb_status rc;
-  if (variant == 2)
-    rc = tma ? launch_c32<true, 256, false, 2>(grid, threads, g.bytes, N, S, K2T, NST, NPL, C,
-                                               d_B32, d_fin, d_Q, d_partial, st)
-             : launch_c32<false, 256, false, 2>(grid, threads, g.bytes, N, S, K2T, NST, NPL, C,
-                                                d_B32, d_fin, d_Q, d_partial, st);
-  else if (hls)
-    rc = tma ? launch_c32<true, 384, true, 8>(grid, threads, g.bytes, N, S, K2T, NST, NPL, C,
-                                              d_B32, d_fin, d_Q, d_partial, st)
-             : launch_c32<false, 384, true, 8>(grid, threads, g.bytes, N, S, K2T, NST, NPL, C,
-                                               d_B32, d_fin, d_Q, d_partial, st);
-  else
-    rc = tma ? launch_c32<true, 256, false, 8>(grid, threads, g.bytes, N, S, K2T, NST, NPL, C,
-                                               d_B32, d_fin, d_Q, d_partial, st)
-             : launch_c32<false, 256, false, 8>(grid, threads, g.bytes, N, S, K2T, NST, NPL, C,
-                                                d_B32, d_fin, d_Q, d_partial, st);
+  edb_status rc =
+      tma ? launch_c32_variant<true>(variant, grid, threads, g.bytes, N, S, K2T, NST, NPL, C, d_B32,
+                                     d_fin, d_Q, d_partial, st)
+          : launch_c32_variant<false>(variant, grid, threads, g.bytes, N, S, K2T, NST, NPL, C,
+                                      d_B32, d_fin, d_Q, d_partial, st);
   if (rc != EDB_OK || C == 1) return rc;
   const long long n = (long long)S * N * N * N;
   const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);

@@ -22,6 +22,8 @@ def main():
     ap.add_argument("--L", type=float, default=7.0)
     ap.add_argument("--mode", type=int, default=1)
     ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--sweep", action="store_true",
+                    help="calq32: time every kernel variant (no chunks and 8 chunks)")
     args = ap.parse_args()
 
     import torch
@@ -39,6 +41,28 @@ def main():
         fh = np.fft.fftn(F0.reshape(S, N, N, N), axes=(1, 2, 3)).reshape(S, -1)
         fin = torch.from_numpy(fh.astype(np.complex64)).cuda()
         out = torch.empty_like(fin)
+        if args.sweep:
+            part = torch.empty(8 * S * N ** 3 * 4, dtype=torch.float32, device="cuda")
+            nv = edb.lib.edb_qcalc_calQ_batch_f32_ex  # noqa: F841 (presence check)
+            for C in (1, 8):
+                for var in range(8):
+                    try:
+                        q.calQ_batch_f32_ex(S, var, C, part, fin, out, stream)
+                    except edb.EdbError as e:
+                        if e.status == 1 and var > 0:
+                            continue
+                        raise
+                    a0 = torch.cuda.Event(enable_timing=True)
+                    a1 = torch.cuda.Event(enable_timing=True)
+                    a0.record(stream)
+                    for _ in range(args.reps):
+                        q.calQ_batch_f32_ex(S, var, C, part, fin, out, stream)
+                    a1.record(stream)
+                    torch.cuda.synchronize()
+                    t = a0.elapsed_time(a1) / args.reps
+                    print(f"variant {var} chunks {C}: {t:.3f} ms, "
+                          f"{10 * float(N) ** 6 * S / (t * 1e-3) / 1e12:.2f} TFLOP/s")
+            del part
         v = q.autotune_batch(S, fin, out, stream)  # 3 launches per variant
         print(f"autotuned variant {v}")
         run = lambda: q.calQ_batch_f32(S, fin, out, stream)  # noqa: E731

@@ -200,8 +200,9 @@ def test_batch_result_same_alone_and_in_the_mix(edb):
 
 @pytest.mark.parametrize("N,L,chunks", [(8, 6.0, 4), (16, 6.0, 8), (24, 7.0, 8)])
 def test_calQ_batch_variants_and_chunks(edb, oracle, N, L, chunks):
-    """Every variant (16- and 4-solve groups, registers / shared memory for
-    the compensated sums) gives bit-identical results for a given chunk count,
+    """Every variant (16- and 4-solve groups, 8 or 4 outputs per thread,
+    registers / shared memory for the compensated sums) gives bit-identical
+    results for a given chunk count,
     a solve alone equals the same solve in a batch, and chunked and unchunked
     results meet the FP32 tolerance (relative L2 <= 5e-6) against the FP64
     oracle."""
@@ -215,12 +216,18 @@ def test_calQ_batch_variants_and_chunks(edb, oracle, N, L, chunks):
     part = torch.empty(chunks * S * N ** 3 * 4, dtype=torch.float32, device="cuda")
     res = {}
     for C in (1, chunks):
-        for v in (0, 1, 2):
+        for v in range(8):
             out = torch.empty_like(fin)
-            q.calQ_batch_f32_ex(S, v, C, part, fin, out)
+            try:
+                q.calQ_batch_f32_ex(S, v, C, part, fin, out)
+            except edb.EdbError as e:  # unknown variant, or one that does not fit this N
+                assert e.status == 1 and v > 0
+                continue
             torch.cuda.synchronize()
             res[(C, v)] = out.cpu().numpy()
-        assert np.array_equal(res[(C, 0)], res[(C, 1)]) and np.array_equal(res[(C, 0)], res[(C, 2)])
+        for (c, v), r in res.items():
+            if c == C:
+                assert np.array_equal(r, res[(C, 0)]), v
         one = torch.empty_like(fin[3:4])
         q.calQ_batch_f32_ex(1, 2, C, part, fin[3:4].contiguous(), one)
         torch.cuda.synchronize()
