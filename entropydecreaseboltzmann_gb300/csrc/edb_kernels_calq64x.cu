@@ -276,6 +276,7 @@ __global__ void __launch_bounds__(256, MINB)
     // and the f_l entry fi = (i3 + sL) mod N, kept in range by one conditional
     int m3n = base3;  // value at i3 = 0
     int fi = fi0;
+    float4 fl_next = __ldg(flrow + fi);
     if (!TMA) {
 #pragma unroll
       for (int a = 0; a < RUN; ++a) bcur[a] = __ldg(brow + colc[a]);
@@ -289,11 +290,12 @@ __global__ void __launch_bounds__(256, MINB)
           const int slot = q % DEPTH;
           mbar_wait(&mybar[slot], (uint32_t)((q / DEPTH) & 1), to);
           const float4 *src = reinterpret_cast<const float4 *>(myring + ((size_t)slot * 32 + lane) * RUN);
-          const float4 v0 = src[0], v1 = src[1];
-          bcur[0] = make_float2(v0.x, v0.y);
-          bcur[1] = make_float2(v0.z, v0.w);
-          bcur[2] = make_float2(v1.x, v1.y);
-          bcur[3] = make_float2(v1.z, v1.w);
+#pragma unroll
+          for (int h = 0; h < RUN / 2; ++h) {
+            const float4 v = src[h];
+            bcur[2 * h] = make_float2(v.x, v.y);
+            bcur[2 * h + 1] = make_float2(v.z, v.w);
+          }
           __syncwarp();
           if (lane == 0 && q + DEPTH < nrows) {  // refill this slot with row q + DEPTH
             const long long lflat = (long long)c0 * N + q + DEPTH;
@@ -315,8 +317,9 @@ __global__ void __launch_bounds__(256, MINB)
           rl[slot] = pk(v.z, v.w);
         }
         // broadcast pairs of f_l.re and f_l.im (hi; and negated hi, lo)
-        const float4 fl = __ldg(flrow + fi);
+        const float4 fl = fl_next;
         fi = (fi + 1 == N) ? 0 : fi + 1;
+        fl_next = __ldg(flrow + fi);
         const u64 xr = pk(fl.x, fl.x), nxr = pk(-fl.x, -fl.x), nlr = pk(-fl.z, -fl.z);
         const u64 xi = pk(fl.y, fl.y), nxi = pk(-fl.y, -fl.y), nli = pk(-fl.w, -fl.w);
 #pragma unroll
