@@ -53,6 +53,19 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, device: str) -> float:
+    """The largest of every rank's x (the job's time is its slowest replica);
+    x itself when no process group is running."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -268,10 +281,7 @@ def main():
     ms = ev0.elapsed_time(ev1)
     clk = clocks.stop()
     launches = edb.kernel_launch_count() - launches0
-    t_ms = torch.tensor([ms], device="cuda")
-    if pg is not None:
-        pg.all_reduce(t_ms, op=pg.ReduceOp.MAX)
-    ms_max = float(t_ms.item())
+    ms_max = max_over_ranks(ms, "cuda")
     evals_per_step = 4 * S
     value = evals_per_step * args.steps * ws / (ms_max * 1e-3)
 

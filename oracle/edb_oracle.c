@@ -415,6 +415,41 @@ int edbo_calQ(int N, int mode, const double *B, const double *fin, double *Qout)
  * [-n, N-1-n].  The idea of an independent direct evaluator follows
  * oldTest/calBBox.h:332-371; the kernel is that of QCalculator.h:181-224.
  * Accumulation order differs from calQ (it runs over k outer, l inner). */
+/* One output mode K (modes in [-n, N-1-n]) of the direct evaluation. */
+static void direct_one(int N, int n, double rval, ftab_t *ft, const double *sig, const double *fin,
+                       int K1, int K2, int K3, double *qr_out, double *qi_out) {
+  double qr = 0.0, qi = 0.0;
+  for (int L1 = -n; L1 < N - n; ++L1)
+    for (int L2 = -n; L2 < N - n; ++L2)
+      for (int L3 = -n; L3 < N - n; ++L3) {
+        int M[3] = {K1 - L1, K2 - L2, K3 - L3};
+        int L[3] = {L1, L2, L3};
+        for (int d = 0; d < 3; ++d) {
+          if (M[d] < -n) M[d] += N;
+          else if (M[d] > N - 1 - n) M[d] -= N;
+        }
+        int a = 0, b = 0, a2 = 0;
+        double sl = 1.0, sm = 1.0;
+        long li = 0, mi = 0;
+        for (int d = 0; d < 3; ++d) {
+          a += (L[d] + M[d]) * (L[d] + M[d]);
+          b += (L[d] - M[d]) * (L[d] - M[d]);
+          a2 += 4 * M[d] * M[d];
+          sl *= sig[L[d] + n];
+          sm *= sig[M[d] + n];
+          li = li * N + (L[d] >= 0 ? L[d] : L[d] + N);
+          mi = mi * N + (M[d] >= 0 ? M[d] : M[d] + N);
+        }
+        double beta = ftab_get(ft, a, b) * sl * sm * rval - ftab_get(ft, a2, 0) * sm * sm * rval;
+        double fr = fin[2 * li], fi = fin[2 * li + 1];
+        double gr = fin[2 * mi], gi = fin[2 * mi + 1];
+        qr += (fr * gr - fi * gi) * beta;
+        qi += (fr * gi + fi * gr) * beta;
+      }
+  *qr_out = qr;
+  *qi_out = qi;
+}
+
 int edbo_direct(int N, double gamma, double R, int filter, const double *fin, double *Qout) {
   const int n = (N - 1) / 2;
   const double rval = edbo_rval(N, gamma, R);
@@ -425,40 +460,32 @@ int edbo_direct(int N, double gamma, double R, int filter, const double *fin, do
   for (int K1 = -n; K1 < N - n; ++K1)
     for (int K2 = -n; K2 < N - n; ++K2)
       for (int K3 = -n; K3 < N - n; ++K3) {
-        double qr = 0.0, qi = 0.0;
-        for (int L1 = -n; L1 < N - n; ++L1)
-          for (int L2 = -n; L2 < N - n; ++L2)
-            for (int L3 = -n; L3 < N - n; ++L3) {
-              int M[3] = {K1 - L1, K2 - L2, K3 - L3};
-              int L[3] = {L1, L2, L3};
-              for (int d = 0; d < 3; ++d) {
-                if (M[d] < -n) M[d] += N;
-                else if (M[d] > N - 1 - n) M[d] -= N;
-              }
-              int a = 0, b = 0, a2 = 0;
-              double sl = 1.0, sm = 1.0;
-              long li = 0, mi = 0;
-              for (int d = 0; d < 3; ++d) {
-                a += (L[d] + M[d]) * (L[d] + M[d]);
-                b += (L[d] - M[d]) * (L[d] - M[d]);
-                a2 += 4 * M[d] * M[d];
-                sl *= sig[L[d] + n];
-                sm *= sig[M[d] + n];
-                li = li * N + (L[d] >= 0 ? L[d] : L[d] + N);
-                mi = mi * N + (M[d] >= 0 ? M[d] : M[d] + N);
-              }
-              double beta = ftab_get(&ft, a, b) * sl * sm * rval -
-                            ftab_get(&ft, a2, 0) * sm * sm * rval;
-              double fr = fin[2 * li], fi = fin[2 * li + 1];
-              double gr = fin[2 * mi], gi = fin[2 * mi + 1];
-              qr += (fr * gr - fi * gi) * beta;
-              qi += (fr * gi + fi * gr) * beta;
-            }
         long ko = ((long)(K1 >= 0 ? K1 : K1 + N) * N + (K2 >= 0 ? K2 : K2 + N)) * N +
                   (K3 >= 0 ? K3 : K3 + N);
-        Qout[2 * ko] = qr;
-        Qout[2 * ko + 1] = qi;
+        direct_one(N, n, rval, &ft, sig, fin, K1, K2, K3, &Qout[2 * ko], &Qout[2 * ko + 1]);
       }
+  free(sig);
+  free(ft.tab);
+  return 0;
+}
+
+/* The direct evaluation at nk chosen output modes, given by FFTW flat index
+ * (kidx), so large N can be checked without the N^6 table: O(nk N^3). */
+int edbo_direct_modes(int N, double gamma, double R, int filter, const double *fin, int nk,
+                      const long *kidx, double *Qout) {
+  const int n = (N - 1) / 2;
+  const double rval = edbo_rval(N, gamma, R);
+  ftab_t ft;
+  if (ftab_init(&ft, N, gamma)) return -1;
+  double *sig = (double *)malloc(sizeof(double) * N);
+  for (int c = 0; c < N; ++c) sig[c] = filter ? edbo_filtering(N, c - n) : 1.0;
+  for (int j = 0; j < nk; ++j) {
+    const long k = kidx[j];
+    int kf[3] = {(int)(k / ((long)N * N)), (int)((k / N) % N), (int)(k % N)};
+    int K[3];
+    for (int d = 0; d < 3; ++d) K[d] = kf[d] > N - 1 - n ? kf[d] - N : kf[d];
+    direct_one(N, n, rval, &ft, sig, fin, K[0], K[1], K[2], &Qout[2 * j], &Qout[2 * j + 1]);
+  }
   free(sig);
   free(ft.tab);
   return 0;

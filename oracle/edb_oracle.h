@@ -39,6 +39,9 @@ int edbo_amax(int N);
 int edbo_genB(int N, double gamma, double R, int filter, int mode, double *B);
 int edbo_calQ(int N, int mode, const double *B, const double *fin, double *Qout);
 int edbo_direct(int N, double gamma, double R, int filter, const double *fin, double *Qout);
+/* edbo_direct at nk output modes given by FFTW flat index; O(nk N^3). */
+int edbo_direct_modes(int N, double gamma, double R, int filter, const double *fin, int nk,
+                      const long *kidx, double *Qout);
 int edbo_calQ_batch_mt(int N, int mode, const double *B, int S, const double *fin,
                        double *Qout, int nthreads);
 long edbo_terms(int N, int mode);

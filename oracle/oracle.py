@@ -66,6 +66,8 @@ class Oracle:
         L.edbo_genB.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, _dp]
         L.edbo_calQ.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp]
         L.edbo_direct.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, _dp, _dp]
+        L.edbo_direct_modes.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, _dp, C.c_int,
+                                        C.POINTER(C.c_long), _dp]
         L.edbo_calQ_batch_mt.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _dp, _dp, C.c_int]
         L.edbo_terms.restype = C.c_long
         L.edbo_terms.argtypes = [C.c_int, C.c_int]
@@ -126,6 +128,18 @@ class Oracle:
         out = np.empty_like(fin)
         rc = self.L.edbo_direct(N, float(gamma), float(R), int(bool(filter)),
                                 _ptr(fin.view(np.float64)), _ptr(out.view(np.float64)))
+        assert rc == 0
+        return out
+
+    def direct_modes(self, N, fin, kidx, gamma=0.0, R=R_REFERENCE, filter=True):
+        """Direct aliased evaluation at the FFTW flat indices kidx (O(len(kidx) N^3))."""
+        fin = np.ascontiguousarray(fin, dtype=np.complex128).reshape(-1)
+        k = np.ascontiguousarray(kidx, dtype=np.int64)
+        out = np.empty(k.size, dtype=np.complex128)
+        rc = self.L.edbo_direct_modes(N, float(gamma), float(R), int(bool(filter)),
+                                      _ptr(fin.view(np.float64)), k.size,
+                                      k.ctypes.data_as(C.POINTER(C.c_long)),
+                                      _ptr(out.view(np.float64)))
         assert rc == 0
         return out
 

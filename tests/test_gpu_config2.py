@@ -1,0 +1,69 @@
+"""The single-solve hard-sphere case at full size: N = 32, L = 8, gamma = 1,
+initial data a seeded mixture of two Maxwellians (mass 0.5 / 0.5, drifts
+U[-2, 2]^3, temperatures U[0.5, 1.5]).
+
+* FP64 drop-in (both kernels) against the oracle's direct evaluation at 96
+  output modes: relative L2 <= 1e-12.  (The oracle's full table would be
+  8.6 GB, so the direct evaluator checks chosen modes exactly.)
+* SSP3 with dt = 0.005 for 200 steps with the entropy fix, FP64 path against
+  the FP32-compensated batched path: the real-space solutions agree to
+  <= 1e-6 of max |f| (the FP32 path's stated accuracy against FP64).
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import INDEX_ALIASED
+
+pytestmark = pytest.mark.gpu
+
+N, L, GAMMA = 32, 8.0, 1.0
+
+
+@pytest.fixture(scope="module")
+def edb():
+    import entropydecreaseboltzmann_gb300 as e
+
+    return e
+
+
+@pytest.fixture(scope="module")
+def f0():
+    from entropydecreaseboltzmann_gb300 import data
+
+    return data.two_maxwellians(N, L, seed=1001)
+
+
+def test_fp64_dropin_N32_gamma1_matches_oracle(edb, oracle, f0):
+    fh = np.fft.fftn(f0.reshape(N, N, N)).reshape(-1)
+    rng = np.random.default_rng(32)
+    kidx = np.unique(np.concatenate([[0, 1, N, N * N, N ** 3 - 1],
+                                     rng.integers(0, N ** 3, 91)]))
+    q = edb.QCalculator(N, 1, L=L, filter=True, index_mode=INDEX_ALIASED)
+    q.genB()
+    want = oracle.direct_modes(N, fh, kidx, gamma=GAMMA, R=L, filter=True)
+    for kind in (0, 1):
+        q.set_fp64_kernel(kind)
+        Q = q.calQ(None, fh)
+        assert np.linalg.norm(Q[kidx] - want) / np.linalg.norm(want) <= 1e-12, kind
+
+
+def test_ssp3_fp32_batched_matches_fp64_N32(edb, f0):
+    dt = 0.005
+    b = edb.BKW3D(N, L, gamma=GAMMA, L=L, filter=True, index_mode=INDEX_ALIASED)
+    b.setFixEntropy(True)
+    b.setInitial(f0)
+    b.SSP3(0.0, 1.0, dt)
+    steps = b.nsteps
+    assert 199 <= steps <= 201
+    # compare the states (the reference's fix rewrites only the real-space output)
+    f64 = np.fft.ifftn(b.Fhat.reshape(N, N, N)).real.reshape(-1)
+    q = edb.QCalculator(N, 1, L=L, filter=True, index_mode=INDEX_ALIASED)
+    q.genB()
+    bs = edb.BatchSolver(q, 1, L, edb.SCHEME_SSP3, dt, fix_entropy=True)
+    bs.load(f0[None, :])
+    bs.step(steps)
+    f32 = bs.read(real=True)[0]
+    err = float(np.max(np.abs(f32 - f64)) / np.max(np.abs(f64)))
+    print(f"N=32 SSP3 x {steps}: FP32-compensated vs FP64, L-inf / max|f| = {err:.3e}")
+    assert err <= 1e-6
+    assert edb.device_status() == 0
