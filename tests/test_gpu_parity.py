@@ -45,9 +45,11 @@ def test_calQ_fp64_matches_reference_golden(edb, golden, N, alpha, filt):
 
 @pytest.mark.parametrize("N", [5, 6, 8, 9])
 @pytest.mark.parametrize("mode", [INDEX_REFERENCE, INDEX_ALIASED])
-@pytest.mark.parametrize("gamma,filt", [(0.0, True), (1.0, False)])
+@pytest.mark.parametrize("gamma,filt", [(0.0, True), (1.0, False), (0.5, False), (0.5, True)])
 def test_genB_matches_oracle(edb, oracle, N, mode, gamma, filt):
-    q = edb.QCalculator(N, int(gamma), L=6.0, filter=filt, index_mode=mode)
+    """gamma 0 and 1: the reference's closed forms; gamma 0.5: the published
+    integral by the same composite Gauss-Legendre rule on both sides."""
+    q = edb.QCalculator(N, int(gamma), gamma=gamma, L=6.0, filter=filt, index_mode=mode)
     q.genB()
     B = q.B()
     Bo = oracle.genB(N, gamma, 6.0, filt, mode)
