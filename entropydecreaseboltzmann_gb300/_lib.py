@@ -43,7 +43,8 @@ class QCalcInfo(C.Structure):
 
 class SolverDesc(C.Structure):
     _fields_ = [("N", C.c_int), ("R", C.c_double), ("scheme", C.c_int), ("fix_entropy", C.c_int),
-                ("beta", C.c_double), ("kernel", QCalcDesc), ("conserve", C.c_int)]
+                ("beta", C.c_double), ("kernel", QCalcDesc), ("conserve", C.c_int),
+                ("record_F", C.c_int)]
 
 
 class BatchDesc(C.Structure):
@@ -129,6 +130,9 @@ def _load():
         "edb_solver_run": (C.c_int, [_vp, C.c_double, C.c_double, C.c_double, _ip]),
         "edb_solver_get": (C.c_int, [_vp, _dp, _dp]),
         "edb_solver_trace": (C.c_int, [_vp, _dp, _dp, C.c_int, _ip]),
+        "edb_solver_F_history": (C.c_int, [_vp, _dp, C.c_int, _ip]),
+        "edb_solver_write_F_dat": (C.c_int, [_vp, C.c_char_p]),
+        "edb_solver_out_v1_direction": (C.c_int, [_vp, C.c_char_p]),
         "edb_batch_create": (C.c_int, [_vp, C.POINTER(BatchDesc), C.POINTER(_vp)]),
         "edb_batch_destroy": (C.c_int, [_vp]),
         "edb_batch_load": (C.c_int, [_vp, _dp]),

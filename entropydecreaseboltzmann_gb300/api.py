@@ -253,8 +253,13 @@ class BKW3D:
     """
 
     def __init__(self, N0: int, R: float, *, gamma: float = 0.0, L: float = R_REFERENCE,
-                 filter: bool = True, index_mode: int = INDEX_REFERENCE, conserve: bool = False):
+                 filter: bool = True, index_mode: int = INDEX_REFERENCE, conserve: bool = False,
+                 record_F: bool = False):
         self.N0 = int(N0)
+        # keep Re F after every step (F_history, write_F_dat)
+        self.record_F = bool(record_F)
+        self.F_history = None
+        self._h = None
         # conservative mode (no reference counterpart): moments projected back
         # after every step, moment-preserving entropy fix fed back into Fhat
         self.conserve = bool(conserve)
@@ -290,8 +295,11 @@ class BKW3D:
         d.kernel.filter = int(self.kernel["filter"])
         d.kernel.index_mode = self.kernel["index_mode"]
         d.conserve = int(self.conserve)
+        d.record_F = int(self.record_F)
+        self._release()
         h = C.c_void_p()
         check(lib.edb_solver_create(C.byref(d), C.byref(h)))
+        ok = False
         try:
             F0p = None if self._F0 is None else dptr(self._F0.view(np.float64))
             check(lib.edb_solver_set_initial(h, F0p))
@@ -307,9 +315,47 @@ class BKW3D:
             n = C.c_int()
             check(lib.edb_solver_trace(h, dptr(raw), dptr(fixed), ns.value, C.byref(n)))
             self.entropy_raw, self.entropy_fixed = raw, fixed
+            if self.record_F:
+                hist = np.empty((ns.value, self.N3d))
+                check(lib.edb_solver_F_history(h, dptr(hist), ns.value, C.byref(n)))
+                self.F_history = hist
+            ok = True
         finally:
-            lib.edb_solver_destroy(h)
+            if ok:
+                self._h = h  # kept for the output writers
+            else:
+                lib.edb_solver_destroy(h)
         return self
+
+    def write_F_dat(self, filename: str = "F.dat"):
+        """The per-step F.dat rows of BKW3D::FEuler (BKW.h:217-249), written in the
+        reference's stream format (needs record_F=True)."""
+        if self._h is None:
+            raise RuntimeError("run an integrator first")
+        check(lib.edb_solver_write_F_dat(self._h, str(filename).encode()))
+
+    def outV1Direction(self, filename: str):
+        """BKW3D::outV1Direction (BKW.h:163-180): x, Re F and funExact along v1
+        through the grid centre, in the reference's format."""
+        if self._h is None:
+            raise RuntimeError("run an integrator first")
+        check(lib.edb_solver_out_v1_direction(self._h, str(filename).encode()))
+
+    @staticmethod
+    def slice_filename(N: int, dt: float) -> str:
+        """testBKW3D.cpp:44: "N" + std::to_string(N) + ".dt" + std::to_string(dt) + ".dat"."""
+        return f"N{int(N)}.dt{float(dt):f}.dat"
+
+    def _release(self):
+        if getattr(self, "_h", None):
+            lib.edb_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self._release()
+        except Exception:
+            pass
 
     def FEuler(self, T0, TEnd, dt):
         return self._run(SCHEME_FE, T0, TEnd, dt)

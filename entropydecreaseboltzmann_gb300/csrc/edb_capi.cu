@@ -5,6 +5,8 @@
 #include <string.h>
 
 #include <atomic>
+#include <fstream>
+#include <iomanip>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -642,6 +644,10 @@ struct edb_solver {
   // conservative mode: moment table, initial moments, forward-DFT scratch
   double *ctab = nullptr, *m0 = nullptr;
   double2 *tmp = nullptr;
+  // record_F: Re F after every step (hist_cap rows of N^3) and the step times
+  double *hist = nullptr;
+  int hist_cap = 0;
+  std::vector<double> times;
 };
 
 extern "C" edb_status edb_solver_create(const edb_solver_desc *d, edb_solver **out) {
@@ -694,6 +700,7 @@ extern "C" edb_status edb_solver_destroy(edb_solver *s) {
   dfree(s->ctab);
   dfree(s->m0);
   dfree(s->tmp);
+  dfree(s->hist);
   if (s->q) edb_qcalc_destroy(s->q);
   if (s->st) cudaStreamDestroy(s->st);
   delete s;
@@ -809,6 +816,7 @@ static edb_status solver_step(edb_solver *s, double dt, bool dufort_startup) {
   }
   if (s->d.scheme == EDB_SCHEME_DUFORT && !dufort_startup)
     EDB_CUDA(cudaMemcpyAsync(s->Fold, F[0], sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+  if (s->hist) EDB_TRY(launch_record_re(n, s->F, s->state, s->hist, s->hist_cap, st));
   return EDB_OK;
 }
 
@@ -824,6 +832,20 @@ extern "C" edb_status edb_solver_run(edb_solver *s, double T0, double TEnd, doub
   s->trace_cap = total;
   EDB_TRY(dalloc(&s->tr_raw, (size_t)total));
   EDB_TRY(dalloc(&s->tr_fixed, (size_t)total));
+  dfree(s->hist);
+  s->hist_cap = 0;
+  if (s->d.record_F) {
+    EDB_TRY(dalloc(&s->hist, (size_t)total * (size_t)n));
+    s->hist_cap = total;
+  }
+  // the step times of the reference loop (t += dt; DUFORT's start-up steps dt/8)
+  s->times.clear();
+  {
+    double t = T0;
+    if (s->d.scheme == EDB_SCHEME_DUFORT)
+      for (int i = 0; i < 8; ++i) s->times.push_back(t += dt / 8);
+    while ((int)s->times.size() < total) s->times.push_back(t += dt);
+  }
   // initial data -> F, Fhat = fft(F) (BKW.h:197-198)
   if (s->has_initial && !s->F0.empty())
     EDB_CUDA(cudaMemcpyAsync(s->F, s->F0.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, st));
@@ -898,6 +920,70 @@ extern "C" edb_status edb_solver_trace(edb_solver *s, double *raw, double *fixed
     EDB_CUDA(cudaMemcpy(fixed, s->tr_fixed, sizeof(double) * k, cudaMemcpyDeviceToHost));
   if (n) *n = s->trace_n;
   return EDB_OK;
+}
+
+extern "C" edb_status edb_solver_F_history(edb_solver *s, double *out, int cap, int *n) {
+  if (!s) return fail(EDB_EINVAL, "null handle");
+  if (!s->hist) return fail(EDB_ENOTREADY, "run with record_F = 1 first");
+  const int k = s->trace_n < cap ? s->trace_n : cap;
+  if (k > 0 && out)
+    EDB_CUDA(cudaMemcpy(out, s->hist, sizeof(double) * (size_t)k * s->NQ, cudaMemcpyDeviceToHost));
+  if (n) *n = s->trace_n;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_solver_write_F_dat(edb_solver *s, const char *path) {
+  if (!s || !path) return fail(EDB_EINVAL, "null argument");
+  if (!s->hist) return fail(EDB_ENOTREADY, "run with record_F = 1 first");
+  const int rows = s->trace_n < s->hist_cap ? s->trace_n : s->hist_cap;
+  std::vector<double> h((size_t)rows * s->NQ);
+  if (rows > 0)
+    EDB_CUDA(cudaMemcpy(h.data(), s->hist, sizeof(double) * h.size(), cudaMemcpyDeviceToHost));
+  // BKW.h:217-249: t, then every Re F, tab-separated, default stream format
+  std::ofstream writeF(path);
+  if (!writeF) return fail(EDB_EINVAL, std::string("cannot open ") + path);
+  for (int r = 0; r < rows; ++r) {
+    writeF << s->times[(size_t)r] << "\t";
+    for (long long i = 0; i < s->NQ; ++i) writeF << h[(size_t)r * s->NQ + i] << "\t";
+    writeF << "\n";
+  }
+  writeF.close();
+  return writeF ? EDB_OK : fail(EDB_EINVAL, std::string("write failed: ") + path);
+}
+
+extern "C" edb_status edb_solver_out_v1_direction(edb_solver *s, const char *path) {
+  if (!s || !path) return fail(EDB_EINVAL, "null argument");
+  const int N0 = s->d.N;
+  const double R = s->d.R;
+  const double h = 2. * R / double(N0);
+  std::vector<double> x((size_t)N0), fval((size_t)N0), F(2 * (size_t)s->NQ);
+  for (int i = 0; i < N0; ++i) x[(size_t)i] = -R + i * h;
+  double *d = nullptr;
+  EDB_TRY(dalloc(&d, 2 * (size_t)N0));
+  cudaError_t e = cudaMemcpy(d, x.data(), sizeof(double) * N0, cudaMemcpyHostToDevice);
+  edb_status rc = e == cudaSuccess
+                      ? launch_funexact_points(R, N0, d, h / 2, h / 2, d + N0, s->st)
+                      : cuda_fail(e, "outV1Direction");
+  if (rc == EDB_OK) {
+    e = cudaMemcpyAsync(fval.data(), d + N0, sizeof(double) * N0, cudaMemcpyDeviceToHost, s->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(F.data(), s->F, sizeof(double2) * s->NQ, cudaMemcpyDeviceToHost, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "outV1Direction");
+  }
+  dfree(d);
+  if (rc != EDB_OK) return rc;
+  // BKW.h:163-180
+  std::ofstream write(path);
+  if (!write) return fail(EDB_EINVAL, std::string("cannot open ") + path);
+  write << "# x\tf(t)\tf_0\n";
+  for (int i = 0; i < N0; ++i) {
+    const long long l = ((long long)i * N0 + N0 / 2) * N0 + N0 / 2;
+    write << std::fixed << std::setprecision(8) << x[(size_t)i] << "\t" << F[2 * (size_t)l] << "\t"
+          << fval[(size_t)i] << "\n";
+  }
+  write.close();
+  return write ? EDB_OK : fail(EDB_EINVAL, std::string("write failed: ") + path);
 }
 
 // ============================================================ batched solves

@@ -170,6 +170,12 @@ edb_status launch_d2f(long long n, const double2 *x, float2 *y, cudaStream_t st)
 edb_status launch_f2d(long long n, const float2 *x, double2 *y, cudaStream_t st);
 edb_status launch_real_to_complex(long long n, const double *x, double2 *y, cudaStream_t st);
 edb_status launch_sinusoid_init(int N, double R, double2 *d_F, cudaStream_t st);
+// BKW3D::funExact's live branch at n points (x[i], y, z).
+edb_status launch_funexact_points(double R, int n, const double *d_x, double y, double z,
+                                  double *d_out, cudaStream_t st);
+// Re F into row (state->rec - 1) of hist (cap rows of N^3 doubles).
+edb_status launch_record_re(long long NQ, const double2 *d_F, const EfixState *d_state,
+                            double *d_hist, int cap, cudaStream_t st);
 // moments (mass, momentum, energy) of Re F per solve, FP64.
 edb_status launch_moments(int N, int batch, double R, const double2 *d_F, double *d_out,
                           cudaStream_t st);

@@ -382,13 +382,8 @@ edb_status launch_real_to_complex(long long n, const double *x, double2 *y, cuda
 }
 
 // setInitialValue with the live funExact branch (BKW.h:96-138).
-__global__ void sinusoid_kernel(int N, double R, double PI, double2 *F) {
-  long long NQ = (long long)N * N * N;
-  long long l = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (l >= NQ) return;
-  int i = (int)(l / ((long long)N * N)), j = (int)((l / N) % N), k = (int)(l % N);
-  double h = 2 * R / (double)N;
-  double x = -R + i * h, y = -R + j * h, z = -R + k * h;
+// BKW3D::funExact, the live branch (BKW.h:96-112): the synthetic sinusoid.
+__device__ double funexact_dev(double R, double PI, double x, double y, double z) {
   double r1 = (x + R) / (2. * R);
   double r2 = (y + R) / (2. * R);
   double r3 = (z + R) / (2. * R);
@@ -397,12 +392,57 @@ __global__ void sinusoid_kernel(int N, double R, double PI, double2 *F) {
     val += fabs((double)jj) / 55 * sin(jj * (r1 - 0.5) * PI) +
            fabs((double)jj) / 55. * sin(jj * (r2 - 0.5) * PI) +
            fabs((double)jj) / 55. * sin(jj * (r3 - 0.5) * PI);
-  F[l] = make_double2(val, 0.0);
+  return val;
+}
+
+__global__ void sinusoid_kernel(int N, double R, double PI, double2 *F) {
+  long long NQ = (long long)N * N * N;
+  long long l = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= NQ) return;
+  int i = (int)(l / ((long long)N * N)), j = (int)((l / N) % N), k = (int)(l % N);
+  double h = 2 * R / (double)N;
+  double x = -R + i * h, y = -R + j * h, z = -R + k * h;
+  F[l] = make_double2(funexact_dev(R, PI, x, y, z), 0.0);
 }
 
 edb_status launch_sinusoid_init(int N, double R, double2 *d_F, cudaStream_t st) {
   long long NQ = (long long)N * N * N;
   sinusoid_kernel<<<(unsigned)((NQ + 255) / 256), 256, 0, st>>>(N, R, M_PI, d_F);
+  EDB_LAUNCHED();
+  return EDB_OK;
+}
+
+// funExact at n points (x[i], y, z) (outV1Direction's reference column).
+__global__ void funexact_points_kernel(double R, double PI, int n, const double *__restrict__ x,
+                                       double y, double z, double *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = funexact_dev(R, PI, x[i], y, z);
+}
+
+edb_status launch_funexact_points(double R, int n, const double *d_x, double y, double z,
+                                  double *d_out, cudaStream_t st) {
+  funexact_points_kernel<<<(n + 127) / 128, 128, 0, st>>>(R, M_PI, n, d_x, y, z, d_out);
+  EDB_LAUNCHED();
+  return EDB_OK;
+}
+
+// Copies Re F into record (rec - 1) of the history: the record the step's
+// entropy rule has just written (the index lives on the device, so a replayed
+// graph fills successive rows).
+__global__ void record_re_kernel(long long NQ, const double2 *__restrict__ F,
+                                 const EfixState *__restrict__ state, double *__restrict__ hist,
+                                 int cap) {
+  const int rec = state->rec - 1;
+  if (rec < 0 || rec >= cap) return;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < NQ;
+       i += (long long)gridDim.x * blockDim.x)
+    hist[(long long)rec * NQ + i] = F[i].x;
+}
+
+edb_status launch_record_re(long long NQ, const double2 *d_F, const EfixState *d_state,
+                            double *d_hist, int cap, cudaStream_t st) {
+  const long long blocks = (NQ + 255) / 256 < 1024 ? (NQ + 255) / 256 : 1024;
+  record_re_kernel<<<(unsigned)blocks, 256, 0, st>>>(NQ, d_F, d_state, d_hist, cap);
   EDB_LAUNCHED();
   return EDB_OK;
 }

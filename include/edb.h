@@ -247,6 +247,8 @@ typedef struct {
                         counterpart): after every step Fhat is projected back onto its initial
                         mass, momentum and energy, and the entropy fix blends toward the discrete
                         Maxwellian of f (moment-preserving) and is fed back into Fhat */
+  int record_F;      /* 1: keep Re F after every step on the device, for edb_solver_F_history
+                        and edb_solver_write_F_dat */
 } edb_solver_desc;
 
 typedef struct edb_solver edb_solver;
@@ -263,6 +265,16 @@ edb_status edb_solver_run(edb_solver *s, double T0, double TEnd, double dt, int 
 edb_status edb_solver_get(edb_solver *s, double *Fhat, double *F);
 /* Entropy after each step before / after the fix (BKW.h:226-235). */
 edb_status edb_solver_trace(edb_solver *s, double *raw, double *fixed, int cap, int *n);
+/* Re F after each step of the last run (record_F = 1): min(cap, steps) rows
+ * of N^3 doubles; *n = steps. */
+edb_status edb_solver_F_history(edb_solver *s, double *out, int cap, int *n);
+/* The reference's output files, written with its stream formats:
+ * F.dat (BKW.h:217-249; one row per step: t, then Re F of every grid point,
+ * tab-separated; needs record_F = 1) and the slice along v1 through the grid
+ * centre (BKW3D::outV1Direction, BKW.h:163-180: x, Re F, funExact(0, x, h/2,
+ * h/2)); testBKW3D.cpp:44-45 names it "N<N>.dt<std::to_string(dt)>.dat". */
+edb_status edb_solver_write_F_dat(edb_solver *s, const char *path);
+edb_status edb_solver_out_v1_direction(edb_solver *s, const char *path);
 
 /* ------------------------------------------- batched solves (FP32 Q-hat) */
 

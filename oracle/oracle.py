@@ -304,6 +304,15 @@ class Reference:
         F = np.ascontiguousarray(F, dtype=np.complex128).reshape(-1)
         return self.L.edbref_bkw_entropy(N, R, _ptr(F.view(np.float64)))
 
+    def fe_files(self, N, R, T0, TEnd, dt, fix, slice_name):
+        """BKW3D::FEuler + outV1Direction of the compiled reference in the
+        current directory: writes F.dat and slice_name there."""
+        self.L.edbref_bkw_fe_files.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double,
+                                               C.c_double, C.c_int, C.c_char_p]
+        rc = self.L.edbref_bkw_fe_files(N, float(R), float(T0), float(TEnd), float(dt),
+                                        int(bool(fix)), slice_name.encode())
+        assert rc == 0
+
     def run(self, N, R, scheme, T0, TEnd, dt, beta=1.0, fix=True, log_cap=1 << 20):
         nq = N ** 3
         Fhat = np.empty(nq, dtype=np.complex128)

@@ -177,6 +177,19 @@ int edbref_bkw_run(int N, double R, int scheme, double T0, double TEnd, double d
   return 0;
 }
 
+// BKW3D::FEuler (BKW.h:191-251), which writes F.dat into the current
+// directory, then outV1Direction(slice) as testBKW3D.cpp:43-45 does; stdout is
+// captured and dropped.
+int edbref_bkw_fe_files(int N, double R, double T0, double TEnd, double dt, int fix_entropy,
+                        const char *slice) {
+  BK b(N, R);
+  b.setFixEntropy(fix_entropy != 0);
+  CoutCapture cap;
+  b.FEuler(T0, TEnd, dt);
+  b.outV1Direction(slice);
+  return 0;
+}
+
 // Times the reference calQ: `reps` calls on the same input; returns seconds
 // per call (steady_clock).  Used only as a CPU baseline where the reference
 // sources exist.

@@ -13,7 +13,10 @@ own CalQ headers and records, for fixed seeds:
 * EntropyFix (EntropyFix.h) on the inputs of CalQ/testEntropyFix.cpp:22-38;
 * the sinusoid initial data (BKW.h:96-138) and calEntropy (:140-152);
 * full BKW3D integrator runs (FE, CFE, RK2, SSP3, RK4, DUFORT) at N = 6,
-  T = 0.05, dt = 0.01, beta = 2: final Fhat, final F and the printed log.
+  T = 0.05, dt = 0.01, beta = 2: final Fhat, final F and the printed log;
+* the reference's output files of that FEuler run, as text beside the .npz:
+  ref_FE_N6_F.dat (BKW.h:217-249) and ref_FE_N6_slice.dat (outV1Direction,
+  BKW.h:163-180).
 
 The FFTs inside those runs come from the in-repo FFTW-API shim, because FFTW
 is not installed here; its conventions are FFTW's documented ones.
@@ -112,6 +115,12 @@ def main():
                 out[f"run_{scheme}_Fhat"] = Fhat
                 out[f"run_{scheme}_F"] = F
                 out[f"run_{scheme}_log"] = np.array(log)
+            # the output files of FEuler + outV1Direction, byte for byte
+            ref.fe_files(6, R, 0.0, 0.05, 0.01, True, "slice.dat")
+            here = os.path.dirname(os.path.abspath(__file__))
+            for src, dst in (("F.dat", "ref_FE_N6_F.dat"), ("slice.dat", "ref_FE_N6_slice.dat")):
+                with open(src, "rb") as fi, open(os.path.join(here, dst), "wb") as fo:
+                    fo.write(fi.read())
         finally:
             os.chdir(cwd)
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_golden.npz")

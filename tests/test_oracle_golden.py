@@ -143,3 +143,19 @@ def test_reference_library_agrees_with_restatement(oracle, reference):
         B = oracle.genB(N, 0.0, R_REFERENCE, True, INDEX_REFERENCE)
         assert np.array_equal(q.B(), B)
         assert np.array_equal(q.calQ(fin), oracle.calQ(N, B, fin, INDEX_REFERENCE))
+
+
+def test_reference_output_files_fixture(reference, tmp_path):
+    """The committed output-file fixtures are exactly what the compiled
+    reference writes for FEuler at N = 6 (F.dat and outV1Direction)."""
+    import os
+
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        reference.fe_files(6, 6.62132, 0.0, 0.05, 0.01, True, "slice.dat")
+    finally:
+        os.chdir(cwd)
+    for got, want in (("F.dat", "ref_FE_N6_F.dat"), ("slice.dat", "ref_FE_N6_slice.dat")):
+        assert (tmp_path / got).read_bytes() == open(os.path.join(here, want), "rb").read()
