@@ -487,9 +487,9 @@ __device__ __forceinline__ void compute_line(const C32Geom &g, const float *Bt, 
 // variant per (table, S).
 template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB>
 __global__ void __launch_bounds__(MAXT, MINB)
-    calq32_kernel(int N, int S, int K2T, int NST, int NPL, int C, const float *__restrict__ B32,
-                  const float2 *__restrict__ fin, float2 *__restrict__ Q,
-                  float4 *__restrict__ partial) {
+    calq32_kernel(int N, int S, int K2T, int NST, int NPL, int C, int GB,
+                  const float *__restrict__ B32, const float2 *__restrict__ fin,
+                  float2 *__restrict__ Q, float4 *__restrict__ partial) {
   constexpr int SG = SC * WS;
   extern __shared__ __align__(128) unsigned char smem[];
   const C32Geom g = c32_geom(N, A, K2T, NST, NPL, HLS ? (int)blockDim.x : 0, SG);
@@ -507,15 +507,26 @@ __global__ void __launch_bounds__(MAXT, MINB)
   const int rest = tid / WS;
   const int r = rest % g.R;
   const int k2l = rest / g.R;
-  const int k1 = blockIdx.y;
-  const int k2_0 = blockIdx.z * K2T;
+  // CTA -> (unit = solve group x chunk, k1, k2 tile).  Blocks of GB units walk
+  // every (k1, tile) before the next block starts, so a block's f-hat stays in
+  // L2 while the table streams once per block (the grid is (units, N, tiles)).
+  const int U = gridDim.x, NT = gridDim.y * gridDim.z;
+  const long long lin =
+      blockIdx.x + (long long)U * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
+  const int blk = (int)(lin / ((long long)GB * NT));
+  const int gsz = min(GB, U - blk * GB);
+  const long long off = lin - (long long)blk * GB * NT;
+  const int kt = (int)(off / gsz);
+  const int unit = blk * GB + (int)(off % gsz);
+  const int k1 = kt % gridDim.y;
+  const int k2_0 = (kt / gridDim.y) * K2T;
   const int k2n = min(K2T, N - k2_0);
   const int k2 = k2_0 + k2l;
   const bool k_ok = (k2l < k2n);
   const int k2c = k_ok ? k2 : k2_0;
   const int k3_0 = r * A;
-  const int chunk = blockIdx.x % C;
-  const int s0 = (blockIdx.x / C) * SG;
+  const int chunk = unit % C;
+  const int s0 = (unit / C) * SG;
   const int nval = min(SG, S - s0);
   // this chunk's l1 planes [P0, P1) and l-lines [li0, li0 + nlines)
   const int PPC = (N + C - 1) / C;
@@ -745,8 +756,8 @@ int calq32_group(int variant) { return SC * kC32Variants[variant].ws; }
 
 template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB>
 static edb_status launch_c32(dim3 grid, int threads, size_t smem, int N, int S, int K2T, int NST,
-                             int NPL, int C, const float *B32, const float2 *fin, float2 *Q,
-                             float4 *partial, cudaStream_t st) {
+                             int NPL, int C, int GB, const float *B32, const float2 *fin,
+                             float2 *Q, float4 *partial, cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(calq32_kernel<TMA, MAXT, HLS, WS, A, MINB>,
@@ -755,31 +766,31 @@ static edb_status launch_c32(dim3 grid, int threads, size_t smem, int N, int S, 
     configured = true;
   }
   calq32_kernel<TMA, MAXT, HLS, WS, A, MINB>
-      <<<grid, threads, smem, st>>>(N, S, K2T, NST, NPL, C, B32, fin, Q, partial);
+      <<<grid, threads, smem, st>>>(N, S, K2T, NST, NPL, C, GB, B32, fin, Q, partial);
   EDB_LAUNCHED();
   return EDB_OK;
 }
 
 template <bool TMA>
 static edb_status launch_c32_variant(int v, dim3 grid, int threads, size_t smem, int N, int S,
-                                     int K2T, int NST, int NPL, int C, const float *B32,
+                                     int K2T, int NST, int NPL, int C, int GB, const float *B32,
                                      const float2 *fin, float2 *Q, float4 *partial,
                                      cudaStream_t st) {
   switch (v) {
     case 1:
-      return launch_c32<TMA, 384, true, 8, 8, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C, B32,
+      return launch_c32<TMA, 384, true, 8, 8, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C, GB, B32,
                                                  fin, Q, partial, st);
     case 2:
-      return launch_c32<TMA, 256, false, 2, 8, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C,
+      return launch_c32<TMA, 256, false, 2, 8, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C, GB,
                                                   B32, fin, Q, partial, st);
     case 3:
-      return launch_c32<TMA, 256, false, 8, 4, 2>(grid, threads, smem, N, S, K2T, NST, NPL, C,
+      return launch_c32<TMA, 256, false, 8, 4, 2>(grid, threads, smem, N, S, K2T, NST, NPL, C, GB,
                                                   B32, fin, Q, partial, st);
     case 4:
-      return launch_c32<TMA, 384, false, 8, 4, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C,
+      return launch_c32<TMA, 384, false, 8, 4, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C, GB,
                                                   B32, fin, Q, partial, st);
     default:
-      return launch_c32<TMA, 256, false, 8, 8, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C,
+      return launch_c32<TMA, 256, false, 8, 8, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C, GB,
                                                   B32, fin, Q, partial, st);
   }
 }
@@ -825,10 +836,14 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   const C32Geom g = c32_geom(N, A, K2T, NST, NPL, hlt, SG);
   if (g.bytes > cap) return fail(EDB_EINVAL, "calq32: this variant does not fit in shared memory");
   dim3 grid((unsigned)(((S + SG - 1) / SG) * C), (unsigned)N, (unsigned)tiles);
+  // solve-group block of the CTA order: about 32 MB of f-hat kept in L2
+  const long long group_bytes = (long long)SG * N * N * N * (long long)sizeof(float2);
+  int GB = (int)std::max<long long>(1, (32LL << 20) / group_bytes) * C;
+  if (GB > (int)grid.x) GB = (int)grid.x;
   edb_status rc =
-      tma ? launch_c32_variant<true>(variant, grid, threads, g.bytes, N, S, K2T, NST, NPL, C, d_B32,
-                                     d_fin, d_Q, d_partial, st)
-          : launch_c32_variant<false>(variant, grid, threads, g.bytes, N, S, K2T, NST, NPL, C,
+      tma ? launch_c32_variant<true>(variant, grid, threads, g.bytes, N, S, K2T, NST, NPL, C, GB,
+                                     d_B32, d_fin, d_Q, d_partial, st)
+          : launch_c32_variant<false>(variant, grid, threads, g.bytes, N, S, K2T, NST, NPL, C, GB,
                                       d_B32, d_fin, d_Q, d_partial, st);
   if (rc != EDB_OK || C == 1) return rc;
   const long long n = (long long)S * N * N * N;
