@@ -44,6 +44,7 @@ METRIC = "batched Q̂ evals/s vs plain FP64 on GB300 at BKW L∞≤1e-6; serve p
 UNIT = "Q̂ evals/s"
 S_BATCH, N_MODES, L_BOX, DT = 4096, 24, 7.0, 0.01
 WORKLOAD = "uniform batch: 4096 solves, N=24, L=7, Maxwell (gamma=0), RK4 dt=0.01, shared B table"
+TRAFFIC_BYTES = 17.64e9 + 0.46e9  # DRAM read + write of one batched-kernel launch (ncu)
 
 
 def dist_env():
@@ -300,6 +301,7 @@ def main():
     torch.cuda.synchronize()
     k_ms = k0.elapsed_time(k1) / kreps
     terms = float(NQ) * NQ * S
+    algo_bytes = 4.0 * NQ * NQ + S * NQ * (8 + 8)  # B32 once, FP32 f-hat in, FP32 Q-hat out
     peak_tf = C_double_peak(edb)
     achieved_tf = 10.0 * terms / (k_ms * 1e-3) / 1e12
 
@@ -387,7 +389,14 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clk,
             "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf,
-                         "unit": "TFLOP/s", "frac": achieved_tf / peak_tf, "traffic": None,
+                         "unit": "TFLOP/s", "frac": achieved_tf / peak_tf,
+                         # dram__bytes_read.sum + dram__bytes_write.sum per launch, one ncu
+                         # capture of this launch (N=24, S=4096, the autotuned variant 3)
+                         "traffic": TRAFFIC_BYTES if S == S_BATCH else None,
+                         "traffic_note": "bytes per launch from ncu; algorithmic bytes are "
+                                         f"{algo_bytes / 1e9:.2f} GB (table once + f-hat in, "
+                                         "Q-hat out): the table streams once per block of "
+                                         "solve groups, and the kernel is FP32-bound",
                          "kernel": "calq32_kernel", "ms_per_launch": k_ms,
                          "flop_per_launch": 10.0 * terms,
                          "peak_source": "FP32 FMA probe measured in this run (edb_measure_fp32_peak)"},
