@@ -121,3 +121,20 @@ def test_ctypes_structs_match_header_layout(tmp_path):
         assert got[(cname, "size")] == C.sizeof(py), cname
         for f, _ in py._fields_:
             assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+def test_server_descriptor_validated_before_device_work():
+    """edb_server_create rejects bad descriptors with EDB_EINVAL before it
+    looks for a GPU."""
+    import ctypes as C
+
+    from entropydecreaseboltzmann_gb300 import _lib
+
+    lib = _lib.lib
+    for field, value in (("scheme", 99), ("dt", 0.0), ("hbm_budget_bytes", -1.0),
+                         ("max_live_per_group", -2)):
+        d = _lib.ServerDesc()
+        d.hbm_budget_bytes, d.scheme, d.dt = 1e9, 4, 0.01
+        setattr(d, field, value)
+        h = C.c_void_p()
+        assert lib.edb_server_create(C.byref(d), C.byref(h)) == 1, field

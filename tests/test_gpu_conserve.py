@@ -184,3 +184,26 @@ def test_batch_conservative_bkw_accuracy(edb):
     f = b.read(real=True)
     exact = np.stack([data.bkw_grid(N, L, t + 50 * dt) for t in t0])
     assert float(np.max(np.abs(f - exact))) <= 1e-6
+
+
+def test_forward_euler_conservative_batch_and_server(edb):
+    """FE (the scheme without stage arrays) in conservative mode with the fix,
+    batched and served: moments kept to 1e-10 relative."""
+    from entropydecreaseboltzmann_gb300 import data
+
+    N, L, S, steps = 12, 6.0, 4, 20
+    f0 = data.maxwellian_mixture_batch(S, N, L, seed=1212)
+    m_init = real_moments(f0, N, L)
+    q = edb.QCalculator(N, 1, L=L, filter=False, index_mode=INDEX_ALIASED)
+    q.genB()
+    b = edb.BatchSolver(q, S, L, edb.SCHEME_FE, 0.005, fix_entropy=True, conserve=True)
+    b.load(f0)
+    b.step(steps)
+    check_conserved(real_moments(b.read(real=True), N, L), m_init)
+    srv = edb.Server(hbm_budget_bytes=4e9, scheme=edb.SCHEME_FE, dt=0.005, fix_entropy=True,
+                     conserve=True)
+    ids = [srv.submit(N, 1.0, L, steps, f0[i], want_result=True) for i in range(S)]
+    srv.run()
+    F = np.stack([srv.result(i)[0] for i in ids])
+    check_conserved(real_moments(F, N, L), m_init)
+    srv.close()

@@ -164,7 +164,8 @@ def _batch_inputs(N, L, S, seed):
     return F0, fh
 
 
-@pytest.mark.parametrize("N,L,S", [(5, 6.0, 3), (8, 6.0, 17), (16, 6.0, 37), (24, 7.0, 20)])
+@pytest.mark.parametrize("N,L,S", [(3, 6.0, 2), (4, 6.0, 5), (5, 6.0, 3), (8, 6.0, 17),
+                                   (16, 6.0, 37), (24, 7.0, 20)])
 def test_calQ_batch_fp32_matches_fp64_oracle(edb, oracle, N, L, S):
     import torch
 
