@@ -77,7 +77,7 @@ class ServerStats(C.Structure):
                 ("qhat_evals", C.c_double), ("qhat_evals_padded", C.c_double),
                 ("qhat_evals_per_s", C.c_double), ("steps_launched", C.c_longlong),
                 ("kernel_launches", C.c_longlong), ("hbm_bytes_peak", C.c_double),
-                ("groups", C.c_int)]
+                ("groups", C.c_int), ("refused", C.c_longlong)]
 
 
 _dp = C.POINTER(C.c_double)
@@ -149,6 +149,9 @@ def _load():
         "edb_server_prepare": (C.c_int, [_vp, C.c_int, C.c_double, C.c_double]),
         "edb_server_submit": (C.c_int, [_vp, C.POINTER(Request), _dp, C.POINTER(C.c_longlong)]),
         "edb_server_run": (C.c_int, [_vp, C.c_double]),
+        "edb_server_start": (C.c_int, [_vp]),
+        "edb_server_stop": (C.c_int, [_vp]),
+        "edb_server_wait": (C.c_int, [_vp, C.c_longlong, C.c_double]),
         "edb_server_result": (C.c_int, [_vp, C.c_longlong, _dp, _dp, C.POINTER(RequestInfo)]),
         "edb_server_get_stats": (C.c_int, [_vp, C.POINTER(ServerStats)]),
         "edb_server_clock": (C.c_int, [_vp, _dp]),

@@ -487,11 +487,24 @@ class Server:
         return rid.value
 
     def run(self, max_wall_s: float = 0.0):
+        """Run the loop on this thread until every submitted request is done."""
         check(lib.edb_server_run(self._h, float(max_wall_s)))
+
+    def start(self):
+        """Run the loop on a background thread; submit() may then be called at any time."""
+        check(lib.edb_server_start(self._h))
+
+    def stop(self):
+        check(lib.edb_server_stop(self._h))
+
+    def wait(self, rid: int, timeout_s: float = 0.0):
+        """Block until request rid is done (timeout_s <= 0: no limit)."""
+        check(lib.edb_server_wait(self._h, int(rid), float(timeout_s)))
 
     def info(self, rid: int) -> dict:
         i = RequestInfo()
         check(lib.edb_server_result(self._h, int(rid), None, None, C.byref(i)))
+        # state: 0 queued, 1 running, 2 done, 3 refused
         return {"state": i.state, "N": i.N, "steps": i.steps, "t_arrival": i.t_arrival,
                 "t_admit": i.t_admit, "t_done": i.t_done}
 

@@ -79,7 +79,7 @@ def build(verbose: bool = False, force: bool = False, extra=None) -> str:
     if failed:
         raise RuntimeError("nvcc failed for: " + ", ".join(failed))
     if force or jobs or _stale(LIB, objs):
-        cmd = [cc, *ARCH, "-shared", "-o", LIB, *objs]
+        cmd = [cc, *ARCH, "-shared", "-o", LIB, *objs, "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stdout + r.stderr)

@@ -31,6 +31,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
 #include <deque>
 #include <map>
 #include <memory>
@@ -52,7 +53,7 @@ struct Req {
   edb_request r;
   std::vector<double> F0;
   double t_arrival = -1, t_admit = -1, t_done = -1;
-  int state = 0;  // 0 queued / not arrived, 1 running, 2 done
+  int state = 0;  // 0 queued / not arrived, 1 running, 2 done, 3 refused (cannot fit)
   int group = -1;
   int remaining = 0;
   std::vector<double> F, Fhat;  // results (want_result)
@@ -113,8 +114,17 @@ struct edb_server {
   Clock::time_point t0;
   long long bytes_used = 0;
   double bytes_peak = 0;
-  long long steps_launched = 0, launches = 0, completed = 0;
+  long long steps_launched = 0, launches = 0, completed = 0, refused = 0;
   double evals = 0, evals_padded = 0;
+  // every field above is guarded by mu once the background loop runs
+  std::mutex mu;
+  std::condition_variable cv_work;  // submissions and stop wake the loop
+  std::condition_variable cv_done;  // completions wake waiters
+  std::thread th;
+  bool started = false, stop_req = false;
+  edb_status loop_status = EDB_OK;
+  std::string loop_msg;
+  int device = 0;
 };
 
 namespace {
@@ -518,6 +528,7 @@ edb_status complete(edb_server *s, Group &g) {
       r.t_done = t;
       ++s->completed;
     }
+    s->cv_done.notify_all();
   }
   // compaction: survivors past the new end move into the holes below it
   const int old_live = g.inflight_live;
@@ -605,6 +616,7 @@ extern "C" edb_status edb_server_create(const edb_server_desc *d, edb_server **o
 
 extern "C" edb_status edb_server_destroy(edb_server *s) {
   if (!s) return EDB_OK;
+  edb_server_stop(s);
   for (auto &g : s->groups) destroy_group(*g);
   delete s;
   return EDB_OK;
@@ -614,6 +626,7 @@ extern "C" edb_status edb_server_prepare(edb_server *s, int N, double gamma, dou
   if (!s) return fail(EDB_EINVAL, "null handle");
   if (N < 3 || N > 64 || !(R > 0) || !(gamma >= 0 && gamma <= 2))
     return fail(EDB_EINVAL, "bad group");
+  std::lock_guard<std::mutex> lk(s->mu);
   int gi = 0;
   return get_group(s, N, gamma, R, &gi);
 }
@@ -629,6 +642,7 @@ extern "C" edb_status edb_server_submit(edb_server *s, const edb_request *r, con
   if (table_bytes_of(r->N) + fixed_bytes_of(r->N) + BUCKET * slot_bytes(s, r->N) >
       (long long)s->d.hbm_budget_bytes)
     return fail(EDB_ENOMEM, "request cannot fit the HBM budget");
+  std::unique_lock<std::mutex> lk(s->mu);
   Req q;
   q.r = *r;
   q.F0.assign(F0_real, F0_real + NQ);
@@ -640,65 +654,56 @@ extern "C" edb_status edb_server_submit(edb_server *s, const edb_request *r, con
   s->reqs.push_back(std::move(q));
   s->pending.push_back(nid);
   if (id) *id = nid;
+  lk.unlock();
+  s->cv_work.notify_one();
   return EDB_OK;
 }
 
-extern "C" edb_status edb_server_run(edb_server *s, double max_wall_s) {
-  if (!s) return fail(EDB_EINVAL, "null handle");
-  if (!s->clock_started) {
-    s->clock_started = true;
-    s->t0 = Clock::now();
+namespace {
+// One pass of the request loop (the caller holds s->mu): arrivals join their
+// group's queue; groups whose step finished retire and compact; queues admit;
+// live groups step.  *busy: work is on the device.  *stuck: requests are
+// queued, nothing runs and none could be admitted (the budget is held by
+// other groups' tables).
+edb_status iterate(edb_server *s, bool *busy, bool *stuck) {
+  const double now = now_s(s);
+  sort_pending(s);
+  while (s->pending_head < s->pending.size()) {
+    const long long id = s->pending[s->pending_head];
+    Req &r = s->reqs[(size_t)id];
+    if (r.t_arrival > now) break;
+    int gi = 0;
+    EDB_TRY(get_group(s, r.r.N, r.r.gamma, r.r.R, &gi));
+    s->groups[(size_t)gi]->queue.push_back(id);
+    ++s->pending_head;
   }
-  const double t_start = now_s(s);
-  for (;;) {
-    const double now = now_s(s);
-    // arrivals
-    sort_pending(s);
-    while (s->pending_head < s->pending.size()) {
-      const long long id = s->pending[s->pending_head];
-      Req &r = s->reqs[(size_t)id];
-      if (r.t_arrival > now) break;
-      int gi = 0;
-      EDB_TRY(get_group(s, r.r.N, r.r.gamma, r.r.R, &gi));
-      s->groups[(size_t)gi]->queue.push_back(id);
-      ++s->pending_head;
-    }
-    bool running = false;
-    for (size_t gi = 0; gi < s->groups.size(); ++gi) {
-      Group &g = *s->groups[gi];
-      if (g.inflight) {
-        cudaError_t e = cudaEventQuery(g.ev);
-        if (e == cudaErrorNotReady) {
-          running = true;
-          continue;
-        }
-        if (e != cudaSuccess) return cuda_fail(e, "server step");
-        g.inflight = false;
-        EDB_TRY(complete(s, g));
-      }
-      if (!g.queue.empty()) EDB_TRY(admit(s, g, (int)gi));
-      if (g.live > 0) {
-        EDB_TRY(tick(s, g));
+  bool running = false, queued = false;
+  for (size_t gi = 0; gi < s->groups.size(); ++gi) {
+    Group &g = *s->groups[gi];
+    if (g.inflight) {
+      cudaError_t e = cudaEventQuery(g.ev);
+      if (e == cudaErrorNotReady) {
         running = true;
+        continue;
       }
+      if (e != cudaSuccess) return cuda_fail(e, "server step");
+      g.inflight = false;
+      EDB_TRY(complete(s, g));
     }
-    if (s->completed == (long long)s->reqs.size()) break;
-    if (max_wall_s > 0 && now_s(s) - t_start > max_wall_s) break;
-    if (running) {
-      std::this_thread::sleep_for(std::chrono::microseconds(20));
-    } else if (s->pending_head < s->pending.size()) {
-      const double next = s->reqs[(size_t)s->pending[s->pending_head]].t_arrival;
-      const double wait = std::min(next - now_s(s), 0.001);
-      if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(wait));
-    } else {
-      bool queued = false;
-      for (auto &g : s->groups) queued |= !g->queue.empty();
-      if (!queued) break;
-      // queued but nothing admitted: the budget is held by nothing live
-      return fail(EDB_ENOMEM, "queued requests cannot be admitted within the HBM budget");
+    if (!g.queue.empty()) EDB_TRY(admit(s, g, (int)gi));
+    if (g.live > 0) {
+      EDB_TRY(tick(s, g));
+      running = true;
     }
+    queued |= !g.queue.empty();
   }
-  // make the results' host copies complete and the streams idle
+  *busy = running;
+  *stuck = !running && queued;
+  return EDB_OK;
+}
+
+// Retires what is still on the device (results to host, streams idle).
+edb_status drain(edb_server *s) {
   for (auto &g : s->groups)
     if (g->inflight) {
       EDB_CUDA(cudaEventSynchronize(g->ev));
@@ -708,9 +713,138 @@ extern "C" edb_status edb_server_run(edb_server *s, double max_wall_s) {
   return EDB_OK;
 }
 
+void start_clock(edb_server *s) {
+  if (!s->clock_started) {
+    s->clock_started = true;
+    s->t0 = Clock::now();
+  }
+}
+
+// The background request loop (edb_server_start).
+void loop_main(edb_server *s) {
+  cudaSetDevice(s->device);
+  std::unique_lock<std::mutex> lk(s->mu);
+  while (!s->stop_req) {
+    bool busy = false, stuck = false;
+    edb_status rc = iterate(s, &busy, &stuck);
+    if (rc == EDB_OK && stuck) {
+      // nothing runs and nothing fits: refuse the head of each blocked queue
+      for (auto &g : s->groups)
+        if (!g->queue.empty() && g->live == 0) {
+          s->reqs[(size_t)g->queue.front()].state = 3;
+          ++s->refused;
+          g->queue.pop_front();
+        }
+      s->cv_done.notify_all();
+    }
+    if (rc != EDB_OK) {
+      s->loop_status = rc;
+      s->loop_msg = edb_last_error();
+      break;
+    }
+    if (busy) {
+      lk.unlock();
+      std::this_thread::sleep_for(std::chrono::microseconds(20));
+      lk.lock();
+    } else {
+      double wait = 0.002;
+      if (s->pending_head < s->pending.size())
+        wait = std::min(wait, s->reqs[(size_t)s->pending[s->pending_head]].t_arrival - now_s(s));
+      if (wait > 0) s->cv_work.wait_for(lk, std::chrono::duration<double>(wait));
+    }
+  }
+  if (s->loop_status == EDB_OK) {
+    edb_status rc = drain(s);
+    if (rc != EDB_OK) {
+      s->loop_status = rc;
+      s->loop_msg = edb_last_error();
+    }
+  }
+  s->cv_done.notify_all();
+}
+}  // namespace
+
+extern "C" edb_status edb_server_run(edb_server *s, double max_wall_s) {
+  if (!s) return fail(EDB_EINVAL, "null handle");
+  std::unique_lock<std::mutex> lk(s->mu);
+  if (s->started) return fail(EDB_EBUSY, "the background loop is running");
+  start_clock(s);
+  const double t_start = now_s(s);
+  for (;;) {
+    bool busy = false, stuck = false;
+    EDB_TRY(iterate(s, &busy, &stuck));
+    if (s->completed + s->refused == (long long)s->reqs.size()) break;
+    if (max_wall_s > 0 && now_s(s) - t_start > max_wall_s) break;
+    if (stuck) return fail(EDB_ENOMEM, "queued requests cannot be admitted within the HBM budget");
+    lk.unlock();
+    if (busy) {
+      std::this_thread::sleep_for(std::chrono::microseconds(20));
+    } else if (s->pending_head < s->pending.size()) {
+      const double next = s->reqs[(size_t)s->pending[s->pending_head]].t_arrival;
+      const double wait = std::min(next - now_s(s), 0.001);
+      if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(wait));
+    }
+    lk.lock();
+  }
+  return drain(s);
+}
+
+extern "C" edb_status edb_server_start(edb_server *s) {
+  if (!s) return fail(EDB_EINVAL, "null handle");
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->started) return fail(EDB_EBUSY, "already started");
+  EDB_CUDA(cudaGetDevice(&s->device));
+  start_clock(s);
+  s->stop_req = false;
+  s->loop_status = EDB_OK;
+  try {
+    s->th = std::thread(loop_main, s);
+  } catch (...) {
+    return fail(EDB_ENOMEM, "cannot start the request loop thread");
+  }
+  s->started = true;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_server_stop(edb_server *s) {
+  if (!s) return fail(EDB_EINVAL, "null handle");
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->started) return EDB_OK;
+    s->stop_req = true;
+  }
+  s->cv_work.notify_all();
+  s->th.join();
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->started = false;
+  if (s->loop_status != EDB_OK) return fail(s->loop_status, s->loop_msg);
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_server_wait(edb_server *s, long long id, double timeout_s) {
+  if (!s) return fail(EDB_EINVAL, "null handle");
+  std::unique_lock<std::mutex> lk(s->mu);
+  if (id < 0 || id >= (long long)s->reqs.size()) return fail(EDB_ENOTFOUND, "unknown request");
+  auto done = [&] {
+    return s->reqs[(size_t)id].state >= 2 || s->loop_status != EDB_OK || !s->started;
+  };
+  if (timeout_s > 0) {
+    if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), done))
+      return fail(EDB_ETIMEDOUT, "request not finished within the timeout");
+  } else {
+    s->cv_done.wait(lk, done);
+  }
+  if (s->loop_status != EDB_OK) return fail(s->loop_status, s->loop_msg);
+  const int st = s->reqs[(size_t)id].state;
+  if (st == 3) return fail(EDB_ENOMEM, "request refused: it cannot fit the HBM budget");
+  if (st != 2) return fail(EDB_ENOTREADY, "the loop stopped before the request finished");
+  return EDB_OK;
+}
+
 extern "C" edb_status edb_server_result(edb_server *s, long long id, double *F_real, double *Fhat,
                                         edb_request_info *info) {
   if (!s) return fail(EDB_EINVAL, "null handle");
+  std::lock_guard<std::mutex> lk(s->mu);
   if (id < 0 || id >= (long long)s->reqs.size()) return fail(EDB_ENOTFOUND, "unknown request");
   const Req &r = s->reqs[(size_t)id];
   if (info) {
@@ -731,12 +865,14 @@ extern "C" edb_status edb_server_result(edb_server *s, long long id, double *F_r
 
 extern "C" edb_status edb_server_clock(edb_server *s, double *t) {
   if (!s || !t) return fail(EDB_EINVAL, "null argument");
+  std::lock_guard<std::mutex> lk(s->mu);
   *t = now_s(s);
   return EDB_OK;
 }
 
 extern "C" edb_status edb_server_get_stats(edb_server *s, edb_server_stats *o) {
   if (!s || !o) return fail(EDB_EINVAL, "null argument");
+  std::lock_guard<std::mutex> lk(s->mu);
   memset(o, 0, sizeof(*o));
   std::vector<double> tts, wait;
   double first = 1e300, last = 0;
@@ -749,7 +885,7 @@ extern "C" edb_status edb_server_get_stats(edb_server *s, edb_server_stats *o) {
       last = std::max(last, r.t_done);
     } else if (r.state == 1) {
       ++live;
-    } else {
+    } else if (r.state == 0) {
       ++queued;
     }
   }
@@ -779,5 +915,6 @@ extern "C" edb_status edb_server_get_stats(edb_server *s, edb_server_stats *o) {
   o->kernel_launches = s->launches;
   o->hbm_bytes_peak = s->bytes_peak;
   o->groups = (int)s->groups.size();
+  o->refused = s->refused;
   return EDB_OK;
 }

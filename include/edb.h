@@ -343,7 +343,8 @@ typedef struct {
 } edb_request;
 
 typedef struct {
-  int state;          /* 0 queued, 1 running, 2 done */
+  int state;          /* 0 queued, 1 running, 2 done, 3 refused (its table and slots could
+                         not be fitted in the budget while nothing else ran) */
   int N, steps;
   double t_arrival, t_admit, t_done; /* server clock, seconds (-1: not yet) */
 } edb_request_info;
@@ -361,6 +362,7 @@ typedef struct {
   long long kernel_launches;  /* kernels in those replays plus admission/retirement work */
   double hbm_bytes_peak;      /* tables + arenas */
   int groups;
+  long long refused;          /* requests refused by the background loop (state 3) */
 } edb_server_stats;
 
 typedef struct edb_server edb_server;
@@ -373,9 +375,19 @@ edb_status edb_server_prepare(edb_server *s, int N, double gamma, double R);
  * its table plus one slot can never fit the budget. */
 edb_status edb_server_submit(edb_server *s, const edb_request *r, const double *F0_real,
                              long long *id);
-/* Runs the request loop until every submitted request is done or
- * max_wall_s seconds (<= 0: no limit) have passed. */
+/* Runs the request loop on the calling thread until every submitted request
+ * is done or max_wall_s seconds (<= 0: no limit) have passed (EDB_EBUSY while
+ * the background loop runs). */
 edb_status edb_server_run(edb_server *s, double max_wall_s);
+/* Runs the request loop on a background host thread until edb_server_stop:
+ * edb_server_submit may then be called from any thread at any time (arrival
+ * < 0 = now), and edb_server_wait blocks until a request is done.  Stop
+ * drains the work on the device; it returns the loop's error, if any. */
+edb_status edb_server_start(edb_server *s);
+edb_status edb_server_stop(edb_server *s);
+/* Waits until request id is done (timeout_s <= 0: no limit): EDB_OK, or
+ * EDB_ETIMEDOUT, or EDB_ENOMEM if it was refused. */
+edb_status edb_server_wait(edb_server *s, long long id, double timeout_s);
 /* f (N^3 doubles) and Fhat (N^3 complex) of a finished request kept with
  * want_result (either pointer may be NULL); info may be NULL. */
 edb_status edb_server_result(edb_server *s, long long id, double *F_real, double *Fhat,

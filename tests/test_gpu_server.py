@@ -173,3 +173,56 @@ def test_uneven_batch_small(edb):
     assert 3 <= st["groups"] <= 9
     assert edb.device_status() == 0
     srv.close()
+
+
+def test_background_loop_serves_concurrent_clients(edb):
+    """edb_server_start: two client threads submit while the loop runs (arrival
+    = now); every result equals the same solve run alone (bit-identical), and a
+    request submitted after the others finished is still served."""
+    import threading
+    import time
+
+    from entropydecreaseboltzmann_gb300 import data
+
+    R, steps = 6.0, 12
+    specs = [(12 if j % 2 else 16, float(j % 3 == 0), 4 + (j % 5)) for j in range(10)]
+    inits = [data.maxwellian_mixture_batch(1, n, R, seed=500 + j)[0]
+             for j, (n, _, _) in enumerate(specs)]
+    # each request alone, through run()
+    alone = []
+    for (n, g, k), f in zip(specs, inits):
+        s1 = edb.Server(hbm_budget_bytes=4e9, scheme=edb.SCHEME_RK4, dt=0.01)
+        rid = s1.submit(n, g, R, steps + k, f, want_result=True)
+        s1.run()
+        alone.append(s1.result(rid)[0])
+        s1.close()
+    srv = edb.Server(hbm_budget_bytes=4e9, scheme=edb.SCHEME_RK4, dt=0.01)
+    srv.start()
+    ids = {}
+    lock = threading.Lock()
+
+    def client(part):
+        for j in range(part, len(specs), 2):
+            n, g, k = specs[j]
+            rid = srv.submit(n, g, R, steps + k, inits[j], want_result=True)
+            with lock:
+                ids[j] = rid
+            time.sleep(0.005)
+
+    ths = [threading.Thread(target=client, args=(p,)) for p in (0, 1)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    for j in range(len(specs)):
+        srv.wait(ids[j], 120.0)
+        F, _ = srv.result(ids[j])
+        assert np.array_equal(F, alone[j]), j
+    # the loop idles, then takes new work
+    late = srv.submit(12, 0.0, R, 3, inits[1], want_result=True)
+    srv.wait(late, 60.0)
+    assert srv.info(late)["state"] == 2
+    srv.stop()
+    st = srv.stats()
+    assert st["completed"] == len(specs) + 1 and st["refused"] == 0
+    srv.close()
