@@ -322,18 +322,21 @@ __global__ void __launch_bounds__(256, MINB)
         fl_next = __ldg(flrow + fi);
         const u64 xr = pk(fl.x, fl.x), nxr = pk(-fl.x, -fl.x), nlr = pk(-fl.z, -fl.z);
         const u64 xi = pk(fl.y, fl.y), nxi = pk(-fl.y, -fl.y), nli = pk(-fl.w, -fl.w);
+        u64 nuh[RUN], ucs[RUN];
 #pragma unroll
         for (int a = 0; a < RUN; ++a) {
           const int slot = (a - t + RUN) % RUN;
           const float bh = bcur[a].x, bl = bcur[a].y;
           const u64 nbh2 = pk(-bh, -bh), bh2 = pk(bh, bh), bl2 = pk(bl, bl);
           // u = b * f_m:  nu_h = -(b_h f_m,h), uc = exact error + cross terms
-          const u64 nu_h = mul2(nbh2, rh[slot]);
-          const u64 ue = fma2(bh2, rh[slot], nu_h);
-          const u64 uc = fma2(bh2, rl[slot], fma2(bl2, rh[slot], ue));
-          df_axpy(accA[a], xr, nxr, nlr, nu_h, uc);
-          df_axpy(accB[a], xi, nxi, nli, nu_h, uc);
+          nuh[a] = mul2(nbh2, rh[slot]);
+          const u64 ue = fma2(bh2, rh[slot], nuh[a]);
+          ucs[a] = fma2(bh2, rl[slot], fma2(bl2, rh[slot], ue));
         }
+#pragma unroll
+        for (int a = 0; a < RUN; ++a) df_axpy(accA[a], xr, nxr, nlr, nuh[a], ucs[a]);
+#pragma unroll
+        for (int a = 0; a < RUN; ++a) df_axpy(accB[a], xi, nxi, nli, nuh[a], ucs[a]);
         if (!TMA) {
 #pragma unroll
           for (int a = 0; a < RUN; ++a) bcur[a] = bnext[a];
