@@ -317,7 +317,7 @@ def main():
     for _ in range(e2e_steps):
         bs.load(h_in.numpy())
         bs.step(1)
-        h_out.numpy()[:] = bs.read(real=True)
+        bs.read(real=True, out=h_out.numpy())
     e2e_s = time.perf_counter() - t0
     e2e_value = evals_per_step * e2e_steps / e2e_s
     h2d = S * NQ * 8

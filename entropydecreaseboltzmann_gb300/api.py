@@ -414,8 +414,15 @@ class BatchSolver:
     def step(self, nsteps=1, stream=None):
         check(lib.edb_batch_step(self._h, int(nsteps), stream_ptr(stream)))
 
-    def read(self, real=True, fhat=False):
-        F = np.empty(self.S * self.NQ) if real else None
+    def read(self, real=True, fhat=False, out=None):
+        """Real-space f (S x N^3) and/or Fhat.  out: a C-contiguous float64 array of
+        S x N^3 to receive f directly (e.g. pinned host memory), instead of a new one."""
+        if real and out is not None:
+            if out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"] or out.size != self.S * self.NQ:
+                raise ValueError("out must be a contiguous float64 array of S x N^3")
+            F = out.reshape(-1)
+        else:
+            F = np.empty(self.S * self.NQ) if real else None
         Fh = np.empty(self.S * self.NQ, dtype=np.complex128) if fhat else None
         check(lib.edb_batch_read(self._h, None if F is None else dptr(F),
                                  None if Fh is None else dptr(Fh.view(np.float64))))

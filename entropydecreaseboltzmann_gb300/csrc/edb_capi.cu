@@ -1092,17 +1092,16 @@ static edb_status batch_init_state(edb_batch *b, cudaStream_t st) {
   return EDB_OK;
 }
 
+// Between steps the first FP32 Q-hat stage array (S x N^3 float2, exactly
+// S x N^3 doubles of bytes) is free; load and read stage real-space data in it.
+static double *batch_staging(edb_batch *b) { return reinterpret_cast<double *>(b->Qs[0]); }
+
 extern "C" edb_status edb_batch_load(edb_batch *b, const double *F0_real) {
   if (!b || !F0_real) return fail(EDB_EINVAL, "null argument");
-  double *tmp = nullptr;
-  EDB_TRY(dalloc(&tmp, (size_t)b->n));
-  cudaError_t e = cudaMemcpyAsync(tmp, F0_real, sizeof(double) * b->n, cudaMemcpyHostToDevice, b->st);
-  edb_status rc = e == cudaSuccess ? launch_real_to_complex(b->n, tmp, b->F, b->st)
-                                   : cuda_fail(e, "cudaMemcpyAsync");
-  if (rc == EDB_OK) rc = batch_init_state(b, b->st);
-  cudaStreamSynchronize(b->st);
-  dfree(tmp);
-  return rc;
+  double *stage = batch_staging(b);
+  EDB_CUDA(cudaMemcpyAsync(stage, F0_real, sizeof(double) * b->n, cudaMemcpyHostToDevice, b->st));
+  EDB_TRY(launch_real_to_complex(b->n, stage, b->F, b->st));
+  return batch_init_state(b, b->st);
 }
 
 extern "C" edb_status edb_batch_load_device(edb_batch *b, const double *d_F0_real, void *stream) {
@@ -1207,14 +1206,14 @@ extern "C" edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat)
   cudaStream_t st = b->st;
   EDB_CUDA(cudaStreamSynchronize(st));
   if (Fhat)
-    EDB_CUDA(cudaMemcpy(Fhat, b->Fhat, sizeof(double2) * b->n, cudaMemcpyDeviceToHost));
-  if (F_real) {
+    EDB_CUDA(cudaMemcpyAsync(Fhat, b->Fhat, sizeof(double2) * b->n, cudaMemcpyDeviceToHost, st));
+  if (F_real) {  // inverse transform, real parts packed on the device
     EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->Fhat, b->F, nullptr, 1, 0, st));
-    std::vector<double2> tmp((size_t)b->n);
-    EDB_CUDA(cudaMemcpyAsync(tmp.data(), b->F, sizeof(double2) * b->n, cudaMemcpyDeviceToHost, st));
-    EDB_CUDA(cudaStreamSynchronize(st));
-    for (long long i = 0; i < b->n; ++i) F_real[i] = tmp[(size_t)i].x;
+    double *stage = batch_staging(b);
+    EDB_TRY(launch_complex_to_real(b->n, b->F, stage, st));
+    EDB_CUDA(cudaMemcpyAsync(F_real, stage, sizeof(double) * b->n, cudaMemcpyDeviceToHost, st));
   }
+  EDB_CUDA(cudaStreamSynchronize(st));
   return EDB_OK;
 }
 

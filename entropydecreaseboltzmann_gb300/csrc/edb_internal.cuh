@@ -169,6 +169,7 @@ edb_status launch_stage_f32q(long long n, int op, double c0, double c1, double c
 edb_status launch_d2f(long long n, const double2 *x, float2 *y, cudaStream_t st);
 edb_status launch_f2d(long long n, const float2 *x, double2 *y, cudaStream_t st);
 edb_status launch_real_to_complex(long long n, const double *x, double2 *y, cudaStream_t st);
+edb_status launch_complex_to_real(long long n, const double2 *y, double *x, cudaStream_t st);
 edb_status launch_sinusoid_init(int N, double R, double2 *d_F, cudaStream_t st);
 // BKW3D::funExact's live branch at n points (x[i], y, z).
 edb_status launch_funexact_points(double R, int n, const double *d_x, double y, double z,

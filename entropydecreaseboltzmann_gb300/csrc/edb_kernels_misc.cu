@@ -375,6 +375,20 @@ edb_status launch_f2d(long long n, const float2 *x, double2 *y, cudaStream_t st)
   EDB_LAUNCHED();
   return EDB_OK;
 }
+// Re y -> x (the inverse of r2c for real data).
+__global__ void c2r_kernel(long long n, const double2 *__restrict__ y, double *__restrict__ x) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] = y[i].x;
+}
+
+edb_status launch_complex_to_real(long long n, const double2 *y, double *x, cudaStream_t st) {
+  const long long blocks = (n + 255) / 256 < 152LL * 32 ? (n + 255) / 256 : 152LL * 32;
+  c2r_kernel<<<(unsigned)blocks, 256, 0, st>>>(n, y, x);
+  EDB_LAUNCHED();
+  return EDB_OK;
+}
+
 edb_status launch_real_to_complex(long long n, const double *x, double2 *y, cudaStream_t st) {
   r2c_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, x, y);
   EDB_LAUNCHED();
