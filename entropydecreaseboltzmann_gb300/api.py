@@ -109,9 +109,11 @@ class QCalculator:
                                                   stream_ptr(stream)))
 
     def calQ_batch_f32_ex(self, S, variant, chunks, d_partial, d_fin, d_Q, stream=None):
-        """Batched kernel with an explicit variant (0, 1: 16-solve groups; 2:
-        4-solve groups) and l1-plane chunk count (d_partial: chunks x S x N^3
-        x 16 bytes on the device when chunks > 1)."""
+        """Batched kernel with an explicit variant (0 .. batch_variants() - 1;
+        0, 1: 16-solve groups; 2: 4-solve groups; 3, 4: 4 outputs per thread;
+        5-9: the same on a solve-pair copy of the input) and l1-plane chunk
+        count (d_partial: chunks x S x N^3 x 16 bytes on the device when
+        chunks > 1)."""
         check(lib.edb_qcalc_calQ_batch_f32_ex(self._h, int(S), int(variant), int(chunks),
                                               devptr(d_partial), devptr(d_fin), devptr(d_Q),
                                               stream_ptr(stream)))

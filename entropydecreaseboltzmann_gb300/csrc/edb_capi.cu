@@ -90,7 +90,21 @@ struct edb_qcalc {
   bool ready = false;
   int c32_variant[16];        // autotuned batched-kernel variant per S class, -1 = untuned
   int c32_variant_split[16];  // the same for chunked launches (serving engine)
+  float4 *pairs = nullptr;    // solve-pair copy of the input for pair variants
+  size_t pairs_bytes = 0;
 };
+
+// Grows the qcalc's solve-pair buffer to hold S solves (not under capture).
+static edb_status qcalc_pairs(edb_qcalc *q, int S) {
+  const size_t need = calq32_pair_bytes(q->d.N, S);
+  if (need <= q->pairs_bytes) return EDB_OK;
+  EDB_CUDA(cudaDeviceSynchronize());
+  dfree(q->pairs);
+  q->pairs_bytes = 0;
+  EDB_TRY(dalloc(&q->pairs, need / sizeof(float4)));
+  q->pairs_bytes = need;
+  return EDB_OK;
+}
 
 // S class of the autotuner: floor(log2(S)), capped at 15.
 static int s_bucket(int S) {
@@ -152,6 +166,7 @@ extern "C" edb_status edb_qcalc_destroy(edb_qcalc *q) {
   dfree(q->B2);
   dfree(q->B32);
   dfree(q->fdf);
+  dfree(q->pairs);
   dfree(q->partial);
   dfree(q->fin);
   dfree(q->Q);
@@ -420,17 +435,19 @@ extern "C" edb_status edb_qcalc_calQ_batch_f32_device(edb_qcalc *q, int S, const
   if (q->d.index_mode != EDB_INDEX_ALIASED)
     return fail(EDB_EINVAL, "the batched path runs the ALIASED index mode");
   if (!q->B32) return fail(EDB_ENOTREADY, "batched calQ before genB");
+  const int v = c32_variant_for(q, S);
+  if (calq32_pair(v)) EDB_TRY(qcalc_pairs(q, S));
   return launch_calq32_batch(q->d.N, S, q->B32, (const float2 *)d_fin, (float2 *)d_Qout,
-                             (cudaStream_t)stream, c32_variant_for(q, S));
+                             (cudaStream_t)stream, v, 1, nullptr, q->pairs);
 }
 
-// Times every variant of the batched kernel on the caller's buffers (two
-// launches each after one warm-up, CUDA events on `stream`) and keeps the
-// fastest for this S bucket.
 // Times every variant of the batched kernel on the caller's buffers (chunk
-// count C, partial buffer for C > 1) and records the fastest for S's class.
+// count C, partial buffer for C > 1; two launches each after one warm-up,
+// CUDA events on `st`) and records the fastest for S's class.  The pair
+// variants take part when the caller passes a pair buffer.
 static edb_status autotune_c32(edb_qcalc *q, int S, const float2 *d_fin, float2 *d_Qout,
-                               cudaStream_t st, int C, float4 *d_partial, int *chosen) {
+                               cudaStream_t st, int C, float4 *d_partial, float4 *d_pairs,
+                               int *chosen) {
   cudaEvent_t e0, e1;
   EDB_CUDA(cudaEventCreate(&e0));
   EDB_CUDA(cudaEventCreate(&e1));
@@ -438,8 +455,9 @@ static edb_status autotune_c32(edb_qcalc *q, int S, const float2 *d_fin, float2 
   float best_ms = 1e30f;
   edb_status rc = EDB_OK;
   for (int v = 0; v < calq32_variants() && rc == EDB_OK; ++v) {
+    if (calq32_pair(v) && !d_pairs) continue;
     if (calq32_group(v) < 16 && S > 64) continue;  // small groups are for few solves
-    rc = launch_calq32_batch(q->d.N, S, q->B32, d_fin, d_Qout, st, v, C, d_partial);
+    rc = launch_calq32_batch(q->d.N, S, q->B32, d_fin, d_Qout, st, v, C, d_partial, d_pairs);
     if (rc == EDB_EINVAL) {  // this variant does not fit this N: skip it
       rc = EDB_OK;
       continue;
@@ -447,7 +465,7 @@ static edb_status autotune_c32(edb_qcalc *q, int S, const float2 *d_fin, float2 
     if (rc != EDB_OK) break;
     cudaEventRecord(e0, st);
     for (int r = 0; r < 2 && rc == EDB_OK; ++r)
-      rc = launch_calq32_batch(q->d.N, S, q->B32, d_fin, d_Qout, st, v, C, d_partial);
+      rc = launch_calq32_batch(q->d.N, S, q->B32, d_fin, d_Qout, st, v, C, d_partial, d_pairs);
     cudaEventRecord(e1, st);
     cudaError_t e = cudaEventSynchronize(e1);
     if (e != cudaSuccess) {
@@ -472,9 +490,11 @@ static edb_status autotune_c32(edb_qcalc *q, int S, const float2 *d_fin, float2 
 namespace edb {
 edb_status qcalc_autotune_split(edb_qcalc *q, int S, const float2 *d_fin, float2 *d_Qout,
                                 cudaStream_t st, int C, float4 *d_partial) {
-  return autotune_c32(q, S, d_fin, d_Qout, st, C, d_partial, nullptr);
+  return autotune_c32(q, S, d_fin, d_Qout, st, C, d_partial, nullptr, nullptr);
 }
 }  // namespace edb
+
+extern "C" int edb_qcalc_batch_variants(void) { return calq32_variants(); }
 
 extern "C" edb_status edb_qcalc_calQ_batch_f32_ex(edb_qcalc *q, int S, int variant, int chunks,
                                                   void *d_partial, const float *d_fin,
@@ -485,8 +505,10 @@ extern "C" edb_status edb_qcalc_calQ_batch_f32_ex(edb_qcalc *q, int S, int varia
   if (chunks < 1 || chunks > q->d.N) return fail(EDB_EINVAL, "chunks must be in [1, N]");
   if (chunks > 1 && !d_partial) return fail(EDB_EINVAL, "chunks > 1 need a partial buffer");
   if (!q->B32) return fail(EDB_ENOTREADY, "batched calQ before genB");
+  if (calq32_pair(variant)) EDB_TRY(qcalc_pairs(q, S));
   return launch_calq32_batch(q->d.N, S, q->B32, (const float2 *)d_fin, (float2 *)d_Qout,
-                             (cudaStream_t)stream, variant, chunks, (float4 *)d_partial);
+                             (cudaStream_t)stream, variant, chunks, (float4 *)d_partial,
+                             q->pairs);
 }
 
 extern "C" edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float *d_fin,
@@ -494,8 +516,9 @@ extern "C" edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float 
   if (!q || !d_fin || !d_Qout) return fail(EDB_EINVAL, "null argument");
   if (S < 1) return fail(EDB_EINVAL, "S must be positive");
   if (!q->B32) return fail(EDB_ENOTREADY, "autotune before genB (ALIASED)");
+  EDB_TRY(qcalc_pairs(q, S));
   return autotune_c32(q, S, (const float2 *)d_fin, (float2 *)d_Qout, (cudaStream_t)stream, 1,
-                      nullptr, chosen);
+                      nullptr, q->pairs, chosen);
 }
 
 extern "C" edb_status edb_device_status(int *status, int clear) {
@@ -997,6 +1020,7 @@ struct edb_batch {
   double2 *Fs[3] = {nullptr, nullptr, nullptr};
   float2 *Qs[4] = {nullptr, nullptr, nullptr, nullptr};
   float2 *in32 = nullptr;
+  float4 *pairs = nullptr;  // solve-pair copy of in32 for the pair variants
   EfixState *state = nullptr;
   double *tr_raw = nullptr, *tr_fixed = nullptr;
   double *mom = nullptr, *H = nullptr;
@@ -1031,6 +1055,7 @@ extern "C" edb_status edb_batch_create(edb_qcalc *q, const edb_batch_desc *d, ed
   for (int i = 0; i < nstage && rc == EDB_OK; ++i) rc = dalloc(&b->Fs[i], n);
   for (int i = 0; i < nq && rc == EDB_OK; ++i) rc = dalloc(&b->Qs[i], n);
   if (rc == EDB_OK) rc = dalloc(&b->in32, n);
+  if (rc == EDB_OK) rc = dalloc(&b->pairs, calq32_pair_bytes(d->N, d->S) / sizeof(float4));
   if (rc == EDB_OK) rc = dalloc(&b->state, (size_t)d->S);
   if (rc == EDB_OK) rc = dalloc(&b->mom, (size_t)d->S * 5);
   if (rc == EDB_OK) rc = dalloc(&b->H, (size_t)d->S);
@@ -1059,6 +1084,7 @@ extern "C" edb_status edb_batch_destroy(edb_batch *b) {
   for (auto &p : b->Fs) dfree(p);
   for (auto &p : b->Qs) dfree(p);
   dfree(b->in32);
+  dfree(b->pairs);
   dfree(b->state);
   dfree(b->mom);
   dfree(b->H);
@@ -1079,8 +1105,7 @@ static edb_status batch_init_state(edb_batch *b, cudaStream_t st) {
   // pick the batched kernel's variant for this S on real data, before the
   // step graph is captured (the graph bakes the choice in)
   if (b->q->c32_variant[s_bucket(b->d.S)] < 0 && !b->exec)
-    EDB_TRY(edb_qcalc_autotune_batch(b->q, b->d.S, (const float *)b->in32, (float *)b->Qs[0], st,
-                                     nullptr));
+    EDB_TRY(autotune_c32(b->q, b->d.S, b->in32, b->Qs[0], st, 1, nullptr, b->pairs, nullptr));
   std::vector<EfixState> init((size_t)b->d.S, EfixState{1.0, 0, 0, 1.0, 0, 0});
   EDB_CUDA(cudaMemcpyAsync(b->state, init.data(), sizeof(EfixState) * b->d.S,
                            cudaMemcpyHostToDevice, st));
@@ -1122,7 +1147,9 @@ static edb_status batch_step_record(edb_batch *b, cudaStream_t st) {
   double2 *Fh = b->Fhat, **F = b->Fs;
   float2 **Q = b->Qs, *in = b->in32;
   const int variant = c32_variant_for(b->q, S);
-  auto calq = [&](float2 *out) { return launch_calq32_batch(N, S, B32, in, out, st, variant); };
+  auto calq = [&](float2 *out) {
+    return launch_calq32_batch(N, S, B32, in, out, st, variant, 1, nullptr, b->pairs);
+  };
   switch (b->d.scheme) {
     case EDB_SCHEME_FE:
       EDB_TRY(calq(Q[0]));

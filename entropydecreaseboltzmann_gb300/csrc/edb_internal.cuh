@@ -115,12 +115,15 @@ edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const float4 *d_
 // Batched FP32 calQ (ALIASED): S solves, B32 in FFTW order.
 // variant in [0, calq32_variants()) selects the solve group and CTA shape
 // (see the kernel).  C > 1 splits the l1 planes into C chunks reduced in
-// order in FP64; d_partial then holds C * S * N^3 float4.
+// order in FP64; d_partial then holds C * S * N^3 float4.  Pair variants
+// (calq32_pair) first copy d_fin into d_pairs, calq32_pair_bytes(N, S) long.
 int calq32_variants();
 int calq32_group(int variant);  // solves per CTA group
+bool calq32_pair(int variant);
+size_t calq32_pair_bytes(int N, int S);
 edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin,
                                float2 *d_Q, cudaStream_t st, int variant, int C = 1,
-                               float4 *d_partial = nullptr);
+                               float4 *d_partial = nullptr, float4 *d_pairs = nullptr);
 // Reads (and optionally clears) the batched kernel's status word: nonzero
 // when a bounded wait inside it ran out.
 edb_status read_calq32_status(int *status, bool clear);

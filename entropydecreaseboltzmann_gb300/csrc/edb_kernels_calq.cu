@@ -205,18 +205,21 @@ __device__ int g_calq32_status;  // nonzero: a bounded wait ran out
 constexpr int MAX_ST = 4;                 // pipeline stages (l-lines in flight)
 
 struct C32Geom {
-  int N, A, R, RA, K2T, BROW, FLS, PSTR, NST, NPL, HLT, SG;
+  int N, A, R, RA, K2T, BROW, FLS, PSTR, NST, NPL, HLT, SG, EL;
   size_t off_B, off_fl, off_pl, off_hl, bytes;
 };
 
 // Shared-memory layout for a CTA: NST stages of (B tile, f_l lines), NPL
 // m1-planes and, when HLT > 0, the compensated (hi, lo) sums of HLT threads
 // (2 * A * SC packed pairs each, thread-fastest so accesses never conflict).
-// Barriers: full[MAX_ST], empty[MAX_ST], plane[2].
+// Barriers: full[MAX_ST], empty[MAX_ST], plane[2].  SG data units (solves, or
+// solve pairs) of EL float2 per element (1: (re, im); 2: (re_a, re_b),
+// (im_a, im_b) of a pair).
 __host__ __device__ inline C32Geom c32_geom(int N, int A, int K2T, int NST, int NPL, int HLT,
-                                            int SG) {
+                                            int SG, int EL = 1) {
   C32Geom g;
   g.SG = SG;
+  g.EL = EL;
   g.A = A;
   g.N = N;
   g.R = (N + A - 1) / A;
@@ -226,8 +229,15 @@ __host__ __device__ inline C32Geom c32_geom(int N, int A, int K2T, int NST, int 
   g.NPL = NPL;
   g.HLT = HLT;
   g.BROW = K2T * N + ROWPAD;
-  g.FLS = g.RA + FLPAD;
-  g.PSTR = N * N + PLPAD;
+  if (EL == 1) {
+    g.FLS = g.RA + FLPAD;
+    g.PSTR = N * N + PLPAD;
+  } else {
+    // 16-byte pair elements: a row stride of 1 mod 8 elements (4 mod 32
+    // words) puts the 8 solve lanes of a quarter-warp on distinct banks
+    g.FLS = (g.RA + (9 - g.RA % 8) % 8) * EL;
+    g.PSTR = (N * N + (9 - (N * N) % 8) % 8) * EL;
+  }
   size_t o = 128;  // 2*MAX_ST + 2 mbarriers (+ pad)
   g.off_B = o;
   o += sizeof(float) * (size_t)NST * g.RA * g.BROW;
@@ -300,8 +310,34 @@ __device__ __forceinline__ u64 pk(float a, float b) {
   asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
   return r;
 }
-__device__ __forceinline__ u64 ld_pk(const float2 *p) {
-  return *reinterpret_cast<const u64 *>(p);
+// Shared-memory loads by 32-bit shared address (explicit ld.shared, so no
+// generic-address resolution in the inner loops)
+__device__ __forceinline__ u64 lds_u64(uint32_t a) {
+  u64 v;
+  asm volatile("ld.shared.u64 %0, [%1];" : "=l"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ ulonglong2 lds_u64x2(uint32_t a) {
+  ulonglong2 v;
+  asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ float4 lds_f4(uint32_t a) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"(a));
+  return v;
+}
+__device__ __forceinline__ float lds_f32(uint32_t a) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ float2 lds_f2(uint32_t a) {
+  float2 v;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
+  return v;
 }
 __device__ __forceinline__ float2 upk(u64 v) {
   float2 r;
@@ -358,25 +394,26 @@ __device__ __forceinline__ void stage_line(const C32Geom &g, int li, int st, int
   float *Bd = Bs + (size_t)st * g.RA * g.BROW;
   float2 *fd = fls + (size_t)st * g.SG * g.FLS;
   const float *Bsrc = B32 + (long long)li * N * NQ + (long long)k1 * N * N + (long long)k2_0 * N;
-  const float2 *fsrc = fin + (long long)s0 * NQ + (long long)li * N;
+  const int EL = g.EL;  // s0 / nval count data units of EL float2 per element
+  const float2 *fsrc = fin + ((long long)s0 * NQ + (long long)li * N) * EL;
   const int rowlen = k2n * N;
   if (TMA) {  // called by warp 0 only
     const int lane = threadIdx.x & 31;
-    if (lane == 0) mbar_expect_tx(full + st, (uint32_t)(N * rowlen * 4 + nval * N * 8));
+    if (lane == 0) mbar_expect_tx(full + st, (uint32_t)(N * rowlen * 4 + nval * N * 8 * EL));
     __syncwarp();
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     for (int l3 = lane; l3 < N; l3 += 32)
       bulk_g2s(Bd + (size_t)l3 * g.BROW, Bsrc + (long long)l3 * NQ, rowlen * 4, full + st);
     for (int s = lane; s < nval; s += 32)
-      bulk_g2s(fd + (size_t)s * g.FLS, fsrc + (long long)s * NQ, N * 8, full + st);
+      bulk_g2s(fd + (size_t)s * g.FLS, fsrc + (long long)s * NQ * EL, N * 8 * EL, full + st);
   } else {
     for (int e = threadIdx.x; e < N * rowlen; e += blockDim.x) {
       int l3 = e / rowlen, c = e % rowlen;
       Bd[(size_t)l3 * g.BROW + c] = __ldg(Bsrc + (long long)l3 * NQ + c);
     }
-    for (int e = threadIdx.x; e < nval * N; e += blockDim.x) {
-      int s = e / N, l3 = e % N;
-      fd[(size_t)s * g.FLS + l3] = __ldg(fsrc + (long long)s * NQ + l3);
+    for (int e = threadIdx.x; e < nval * N * EL; e += blockDim.x) {
+      int s = e / (N * EL), j = e % (N * EL);
+      fd[(size_t)s * g.FLS + j] = __ldg(fsrc + (long long)s * NQ * EL + j);
     }
   }
 }
@@ -385,19 +422,19 @@ template <bool TMA>
 __device__ __forceinline__ void stage_plane(const C32Geom &g, int m1, int s0, int nval,
                                             long long NQ, const float2 *__restrict__ fin,
                                             float2 *pl, uint64_t *bar) {
-  const int NN = g.N * g.N;
-  const float2 *src = fin + (long long)s0 * NQ + (long long)m1 * NN;
+  const int NN = g.N * g.N, EL = g.EL;
+  const float2 *src = fin + ((long long)s0 * NQ + (long long)m1 * NN) * EL;
   if (TMA) {  // warp 0 only
     const int lane = threadIdx.x & 31;
-    if (lane == 0) mbar_expect_tx(bar, (uint32_t)(nval * NN * 8));
+    if (lane == 0) mbar_expect_tx(bar, (uint32_t)(nval * NN * 8 * EL));
     __syncwarp();
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     for (int s = lane; s < nval; s += 32)
-      bulk_g2s(pl + (size_t)s * g.PSTR, src + (long long)s * NQ, NN * 8, bar);
+      bulk_g2s(pl + (size_t)s * g.PSTR, src + (long long)s * NQ * EL, NN * 8 * EL, bar);
   } else {
-    for (int e = threadIdx.x; e < nval * NN; e += blockDim.x) {
-      int s = e / NN, p = e % NN;
-      pl[(size_t)s * g.PSTR + p] = __ldg(src + (long long)s * NQ + p);
+    for (int e = threadIdx.x; e < nval * NN * EL; e += blockDim.x) {
+      int s = e / (NN * EL), p = e % (NN * EL);
+      pl[(size_t)s * g.PSTR + p] = __ldg(src + (long long)s * NQ * EL + p);
     }
   }
 }
@@ -413,6 +450,8 @@ __device__ __forceinline__ void compute_line(const C32Geom &g, const float *Bt, 
                                              const float2 *p1, int k3_0, u64 (&accA)[A][SC],
                                              u64 (&accB)[A][SC]) {
   const int N = g.N;
+  const uint32_t sp0 = s_addr(p0), sp1 = s_addr(p1), sf0 = s_addr(fl0), sf1 = s_addr(fl1);
+  const uint32_t sB = s_addr(Bt), brow = 4u * g.BROW;
   u64 ring[A][SC];
 #pragma unroll
   for (int a = 0; a < A; ++a) {
@@ -422,8 +461,8 @@ __device__ __forceinline__ void compute_line(const C32Geom &g, const float *Bt, 
     } else {
       while (idx >= N) idx -= N;
     }
-    ring[a][0] = ld_pk(p0 + idx);
-    ring[a][1] = ld_pk(p1 + idx);
+    ring[a][0] = lds_u64(sp0 + 8u * idx);
+    ring[a][1] = lds_u64(sp1 + 8u * idx);
   }
   for (int gg = 0; gg < g.R; ++gg) {
     int base = k3_0 - gg * A;
@@ -443,14 +482,14 @@ __device__ __forceinline__ void compute_line(const C32Geom &g, const float *Bt, 
           while (idx < 0) idx += N;
         }
         const int slot = (A - t) % A;
-        ring[slot][0] = ld_pk(p0 + idx);
-        ring[slot][1] = ld_pk(p1 + idx);
+        ring[slot][0] = lds_u64(sp0 + 8u * idx);
+        ring[slot][1] = lds_u64(sp1 + 8u * idx);
       }
       float bv[A];
       if (VEC) {
 #pragma unroll
         for (int q4 = 0; q4 < A / 4; ++q4) {
-          const float4 b = *reinterpret_cast<const float4 *>(Bt + (size_t)l3 * g.BROW + 4 * q4);
+          const float4 b = lds_f4(sB + brow * l3 + 16u * q4);
           bv[4 * q4] = b.x;
           bv[4 * q4 + 1] = b.y;
           bv[4 * q4 + 2] = b.z;
@@ -458,9 +497,9 @@ __device__ __forceinline__ void compute_line(const C32Geom &g, const float *Bt, 
         }
       } else {
 #pragma unroll
-        for (int a = 0; a < A; ++a) bv[a] = Bt[(size_t)l3 * g.BROW + a];
+        for (int a = 0; a < A; ++a) bv[a] = lds_f32(sB + brow * l3 + 4u * a);
       }
-      const float2 f0 = fl0[l3], f1 = fl1[l3];
+      const float2 f0 = lds_f2(sf0 + 8u * l3), f1 = lds_f2(sf1 + 8u * l3);
       const u64 flx[SC] = {pk(f0.x, f0.x), pk(f1.x, f1.x)};
       const u64 fly[SC] = {pk(f0.y, f0.y), pk(f1.y, f1.y)};
 #pragma unroll
@@ -477,22 +516,111 @@ __device__ __forceinline__ void compute_line(const C32Geom &g, const float *Bt, 
     }
   }
 }
+
+// compute_line for a solve pair (PAIR layout: element = (re_a, re_b),
+// (im_a, im_b)).  The packed lanes are the two solves, so f_l and f_m need no
+// broadcast and one 16-byte load brings both components of both solves.  The
+// four sums per output keep the per-solve operation order of compute_line:
+//   accA[a][0] = sum f_l.re q.re    accA[a][1] = sum f_l.re q.im
+//   accB[a][0] = sum f_l.im q.re    accB[a][1] = sum f_l.im q.im
+// (lanes = solves), so both layouts give the same bits.
+template <bool BIGN, bool VEC, int A>
+__device__ __forceinline__ void compute_line_pair(const C32Geom &g, const float *Bt,
+                                                  const float2 *fl, const float2 *p, int k3_0,
+                                                  u64 (&accA)[A][SC], u64 (&accB)[A][SC]) {
+  const int N = g.N;
+  const uint32_t sp = s_addr(p), sf = s_addr(fl), sB = s_addr(Bt), brow = 4u * g.BROW;
+  ulonglong2 ring[A];
+#pragma unroll
+  for (int a = 0; a < A; ++a) {
+    int idx = k3_0 + a;
+    if (BIGN) {
+      idx -= (idx >= N) ? N : 0;
+    } else {
+      while (idx >= N) idx -= N;
+    }
+    ring[a] = lds_u64x2(sp + 16u * idx);
+  }
+  for (int gg = 0; gg < g.R; ++gg) {
+    int base = k3_0 - gg * A;
+    if (BIGN) {
+      base += (base < 0) ? N : 0;
+    } else {
+      while (base < 0) base += N;
+    }
+#pragma unroll
+    for (int t = 0; t < A; ++t) {
+      const int l3 = gg * A + t;
+      if (t > 0 || gg > 0) {
+        int idx = base - t;
+        if (BIGN) {
+          idx += (idx < 0) ? N : 0;
+        } else {
+          while (idx < 0) idx += N;
+        }
+        ring[(A - t) % A] = lds_u64x2(sp + 16u * idx);
+      }
+      float bv[A];
+      if (VEC) {
+#pragma unroll
+        for (int q4 = 0; q4 < A / 4; ++q4) {
+          const float4 b = lds_f4(sB + brow * l3 + 16u * q4);
+          bv[4 * q4] = b.x;
+          bv[4 * q4 + 1] = b.y;
+          bv[4 * q4 + 2] = b.z;
+          bv[4 * q4 + 3] = b.w;
+        }
+      } else {
+#pragma unroll
+        for (int a = 0; a < A; ++a) bv[a] = lds_f32(sB + brow * l3 + 4u * a);
+      }
+      const ulonglong2 f = lds_u64x2(sf + 16u * l3);
+#pragma unroll
+      for (int a = 0; a < A; ++a) {
+        const ulonglong2 m = ring[(a - t + A) % A];
+        const u64 bb = pk(bv[a], bv[a]);
+        const u64 qr = mul2(bb, m.x), qi = mul2(bb, m.y);
+        fma2(accA[a][0], f.x, qr);
+        fma2(accA[a][1], f.x, qi);
+        fma2(accB[a][0], f.y, qr);
+        fma2(accB[a][1], f.y, qi);
+      }
+    }
+  }
+}
+
+// Solve pairs for the PAIR variants: out[P][e] = (re_2P, re_2P+1, im_2P,
+// im_2P+1); a missing odd partner reads as zero.
+__global__ void c32_pairs_kernel(int S, long long NQ, const float2 *__restrict__ fin,
+                                 float4 *__restrict__ out) {
+  const long long n = (long long)((S + 1) / 2) * NQ;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long P = i / NQ, e = i - P * NQ;
+    const float2 a = __ldg(fin + 2 * P * NQ + e);
+    const float2 b = (2 * P + 1 < S) ? __ldg(fin + (2 * P + 1) * NQ + e) : make_float2(0.f, 0.f);
+    out[i] = make_float4(a.x, b.x, a.y, b.y);
+  }
+}
 }  // namespace
 
 // MAXT bounds the CTA size: 256 threads keep at most two warps per SM
 // sub-partition, so up to 255 registers per thread; 384 allow more warps at
 // 168 registers.  HLS: keep the compensated (hi, lo) pairs in shared memory
 // instead of registers, which frees 64 registers per thread for more resident
-// warps.  WS: solve lanes (group of 2 WS solves).  The autotuner picks the
-// variant per (table, S).
-template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB>
+// warps.  WS: solve lanes (group of 2 WS solves).  PAIR: fin is in the
+// solve-pair layout (c32_pairs_kernel) and lane w holds solves 2w, 2w+1 of
+// the group; otherwise fin is plain and lane w holds solves w, w+WS.  The
+// autotuner picks the variant per (table, S).
+template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB, bool PAIR>
 __global__ void __launch_bounds__(MAXT, MINB)
     calq32_kernel(int N, int S, int K2T, int NST, int NPL, int C, int GB,
                   const float *__restrict__ B32, const float2 *__restrict__ fin,
                   float2 *__restrict__ Q, float4 *__restrict__ partial) {
-  constexpr int SG = SC * WS;
+  constexpr int SG = SC * WS;  // solves per group
   extern __shared__ __align__(128) unsigned char smem[];
-  const C32Geom g = c32_geom(N, A, K2T, NST, NPL, HLS ? (int)blockDim.x : 0, SG);
+  const C32Geom g =
+      c32_geom(N, A, K2T, NST, NPL, HLS ? (int)blockDim.x : 0, PAIR ? WS : SG, PAIR ? 2 : 1);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);  // [MAX_ST]
   uint64_t *empty = full + MAX_ST;                       // [MAX_ST]
   uint64_t *pbar = full + 2 * MAX_ST;                    // [2] planes
@@ -527,13 +655,15 @@ __global__ void __launch_bounds__(MAXT, MINB)
   const int k3_0 = r * A;
   const int chunk = unit % C;
   const int s0 = (unit / C) * SG;
-  const int nval = min(SG, S - s0);
+  // staged data units (solves, or solve pairs) of this group
+  const int u0 = PAIR ? s0 / 2 : s0;
+  const int nval = PAIR ? min(WS, (S - s0 + 1) / 2) : min(SG, S - s0);
   // this chunk's l1 planes [P0, P1) and l-lines [li0, li0 + nlines)
   const int PPC = (N + C - 1) / C;
   const int P0 = min(N, chunk * PPC), P1 = min(N, P0 + PPC);
   const int nplanes = P1 - P0;
   const int li0 = P0 * N, nlines = nplanes * N;
-  const size_t plane_sz = (size_t)SG * g.PSTR;
+  const size_t plane_sz = (size_t)g.SG * g.PSTR;
 
   // zero the tile/line buffers once: padded rows (l3 >= N), row tails and the
   // f_l tails are never written by the copies and must read as zeros
@@ -569,15 +699,15 @@ __global__ void __launch_bounds__(MAXT, MINB)
         lo[HLS ? 0 : a][c] = 0ull;
       }
     }
-  const u64 neg_re = pk(-1.f, 1.f);
+  const u64 neg_re = pk(-1.f, 1.f), neg_one = pk(-1.f, -1.f);
 
   // Pipeline bookkeeping uses chunk-relative indices: j (line), pr (plane).
   // prologue: lines 0 .. NST-2 and the first plane
   int issued = 0, planes = 0;  // counted in warp 0
   if (TMA && warp == 0 && nlines > 0) {
     for (int j = 0; j < NST - 1 && j < nlines; ++j, ++issued)
-      stage_line<true>(g, li0 + j, j % NST, k1, k2_0, k2n, s0, nval, NQ, B32, fin, Bs, fls, full);
-    stage_plane<true>(g, (k1 - P0 + N) % N, s0, nval, NQ, fin, plb, &pbar[0]);
+      stage_line<true>(g, li0 + j, j % NST, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full);
+    stage_plane<true>(g, (k1 - P0 + N) % N, u0, nval, NQ, fin, plb, &pbar[0]);
     ++planes;
   }
   bool to = false;
@@ -597,20 +727,20 @@ __global__ void __launch_bounds__(MAXT, MINB)
       if (TMA) {
         if (NPL == 2) {
           if (warp == 0 && pr + 1 < nplanes) {
-            stage_plane<true>(g, (k1 - (l1 + 1) + N) % N, s0, nval, NQ, fin,
+            stage_plane<true>(g, (k1 - (l1 + 1) + N) % N, u0, nval, NQ, fin,
                               plb + (size_t)((pr + 1) & 1) * plane_sz, &pbar[(pr + 1) & 1]);
             ++planes;
           }
           mbar_wait(&pbar[pr & 1], (uint32_t)((pr >> 1) & 1), to);
         } else {
           if (warp == 0 && pr > 0) {
-            stage_plane<true>(g, (k1 - l1 + N) % N, s0, nval, NQ, fin, plb, &pbar[0]);
+            stage_plane<true>(g, (k1 - l1 + N) % N, u0, nval, NQ, fin, plb, &pbar[0]);
             ++planes;
           }
           mbar_wait(&pbar[0], (uint32_t)(pr & 1), to);
         }
       } else {
-        stage_plane<false>(g, (k1 - l1 + N) % N, s0, nval, NQ, fin, plb, pbar);
+        stage_plane<false>(g, (k1 - l1 + N) % N, u0, nval, NQ, fin, plb, pbar);
       }
     }
     if (TMA) {
@@ -619,38 +749,52 @@ __global__ void __launch_bounds__(MAXT, MINB)
       if (warp == 0 && jn < nlines) {
         const int sn = jn % NST;
         if (j >= 1) mbar_wait(&empty[sn], (uint32_t)(((j - 1) / NST) & 1), to);
-        stage_line<true>(g, li0 + jn, sn, k1, k2_0, k2n, s0, nval, NQ, B32, fin, Bs, fls, full);
+        stage_line<true>(g, li0 + jn, sn, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full);
         ++issued;
       }
       mbar_wait(&full[st], (uint32_t)((j / NST) & 1), to);
     } else {
       __syncthreads();  // previous line's readers are done (single buffer)
-      stage_line<false>(g, li, st, k1, k2_0, k2n, s0, nval, NQ, B32, fin, Bs, fls, full);
+      stage_line<false>(g, li, st, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full);
       __syncthreads();
     }
 
     // ---- compute line (l1, l2)
     const int m2 = (k2c - l2 + N) % N;
     const float *Bt = Bs + (size_t)st * g.RA * g.BROW + k2l * N + k3_0;
-    const float2 *fl0 = fls + (size_t)st * SG * g.FLS + (size_t)w * g.FLS;
-    const float2 *fl1 = fl0 + (size_t)WS * g.FLS;
-    const float2 *p0 = plb + (size_t)pb * plane_sz + (size_t)w * g.PSTR + m2 * N;
-    const float2 *p1 = p0 + (size_t)WS * g.PSTR;
-    if (TMA)
-      compute_line<true, true, A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
-    else
-      compute_line<false, false, A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
+    const float2 *fl0 = fls + (size_t)st * g.SG * g.FLS + (size_t)w * g.FLS;
+    const float2 *p0 = plb + (size_t)pb * plane_sz + (size_t)w * g.PSTR + m2 * N * g.EL;
+    if (PAIR) {
+      if (TMA)
+        compute_line_pair<true, true, A>(g, Bt, fl0, p0, k3_0, accA, accB);
+      else
+        compute_line_pair<false, false, A>(g, Bt, fl0, p0, k3_0, accA, accB);
+    } else {
+      const float2 *fl1 = fl0 + (size_t)WS * g.FLS;
+      const float2 *p1 = p0 + (size_t)WS * g.PSTR;
+      if (TMA)
+        compute_line<true, true, A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
+      else
+        compute_line<false, false, A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
+    }
     if (TMA) {
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[st]);
     }
     if ((l2 + 1) % FOLD_LINES == 0 || l2 == N - 1) {  // fold into the compensated pair
 #pragma unroll
-      for (int a = 0; a < A; ++a)
+      for (int a = 0; a < A; ++a) {
+        // (accA.x - accB.y, accA.y + accB.x) = accA + (-1, 1) * swap(accB);
+        // PAIR: xs[0] the real parts, xs[1] the imaginary parts of both solves
+        u64 xs[SC];
+#pragma unroll
+        for (int c = 0; c < SC; ++c)
+          xs[c] = !PAIR ? fma2r(neg_re, swp(accB[a][c]), accA[a][c])
+                  : c == 0 ? fma2r(neg_one, accB[a][1], accA[a][0])
+                           : add2(accA[a][1], accB[a][0]);
 #pragma unroll
         for (int c = 0; c < SC; ++c) {
-          // (accA.x - accB.y, accA.y + accB.x) = accA + (-1, 1) * swap(accB)
-          const u64 x = fma2r(neg_re, swp(accB[a][c]), accA[a][c]);
+          const u64 x = xs[c];
           if (HLS) {
             u64 *ph = hl + (size_t)(2 * (a * SC + c)) * blockDim.x + tid;
             u64 h = ph[0], l = ph[blockDim.x];
@@ -663,6 +807,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
           accA[a][c] = 0ull;
           accB[a][c] = 0ull;
         }
+      }
     }
   }
   if (!aborted && __syncthreads_or(to)) aborted = true;
@@ -695,22 +840,37 @@ __global__ void __launch_bounds__(MAXT, MINB)
   if (!k_ok) return;
 #pragma unroll
   for (int c = 0; c < SC; ++c) {
-    const int s = s0 + w + c * WS;
+    const int s = PAIR ? s0 + 2 * w + c : s0 + w + c * WS;
     if (s >= S) continue;
     const long long o = (long long)k1 * N * N + (long long)k2 * N;
 #pragma unroll
     for (int a = 0; a < A; ++a) {
       const int k3 = k3_0 + a;
       if (k3 < N) {
-        u64 hv, lv;
-        if (HLS) {
-          hv = hl[(size_t)(2 * (a * SC + c)) * blockDim.x + tid];
-          lv = hl[(size_t)(2 * (a * SC + c) + 1) * blockDim.x + tid];
-        } else {
-          hv = hi[HLS ? 0 : a][c];
-          lv = lo[HLS ? 0 : a][c];
+        // (hi, lo) of this output: packed (re, im) at [a][c], or for PAIR
+        // lane c of the packed real [a][0] and imaginary [a][1] sums
+        u64 hv[SC], lv[SC];
+#pragma unroll
+        for (int j = 0; j < SC; ++j) {
+          if (PAIR || j == c) {
+            if (HLS) {
+              hv[j] = hl[(size_t)(2 * (a * SC + j)) * blockDim.x + tid];
+              lv[j] = hl[(size_t)(2 * (a * SC + j) + 1) * blockDim.x + tid];
+            } else {
+              hv[j] = hi[HLS ? 0 : a][j];
+              lv[j] = lo[HLS ? 0 : a][j];
+            }
+          }
         }
-        const float2 h = upk(hv), l = upk(lv);
+        float2 h, l;
+        if (PAIR) {
+          const float2 hr = upk(hv[0]), hm = upk(hv[1]), lr = upk(lv[0]), lm = upk(lv[1]);
+          h = c == 0 ? make_float2(hr.x, hm.x) : make_float2(hr.y, hm.y);
+          l = c == 0 ? make_float2(lr.x, lm.x) : make_float2(lr.y, lm.y);
+        } else {
+          h = upk(hv[c]);
+          l = upk(lv[c]);
+        }
         if (C == 1)
           Q[(long long)s * NQ + o + k3] = make_float2(h.x + l.x, h.y + l.y);
         else
@@ -743,29 +903,36 @@ __global__ void calq32_reduce_kernel(long long n, int C, const float4 *__restric
 //   2: WS 2, A 8, <= 256 threads, registers        (4-solve groups)
 //   3: WS 8, A 4, <= 256 threads, registers, 2 CTAs per SM (<= 128 registers)
 //   4: WS 8, A 4, <= 384 threads, registers (<= 168 registers)
+//   5-9: 0-4 on the solve-pair layout (same bits, fewer operand moves and
+//        shared-memory loads; needs a pair-layout copy of the input)
 struct C32Variant {
   int ws, a, maxt;
   bool hls;
   int minb;
+  bool pair;
 };
 constexpr C32Variant kC32Variants[] = {
-    {8, 8, 256, false, 1}, {8, 8, 384, true, 1}, {2, 8, 256, false, 1},
-    {8, 4, 256, false, 2}, {8, 4, 384, false, 1}};
+    {8, 8, 256, false, 1, false}, {8, 8, 384, true, 1, false}, {2, 8, 256, false, 1, false},
+    {8, 4, 256, false, 2, false}, {8, 4, 384, false, 1, false}, {8, 8, 256, false, 1, true},
+    {8, 8, 384, true, 1, true},   {2, 8, 256, false, 1, true},  {8, 4, 256, false, 2, true},
+    {8, 4, 384, false, 1, true}};
 int calq32_variants() { return (int)(sizeof(kC32Variants) / sizeof(kC32Variants[0])); }
 int calq32_group(int variant) { return SC * kC32Variants[variant].ws; }
+bool calq32_pair(int variant) { return kC32Variants[variant].pair; }
+size_t calq32_pair_bytes(int N, int S) { return (size_t)((S + 1) / 2) * N * N * N * sizeof(float4); }
 
-template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB>
+template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB, bool PAIR>
 static edb_status launch_c32(dim3 grid, int threads, size_t smem, int N, int S, int K2T, int NST,
                              int NPL, int C, int GB, const float *B32, const float2 *fin,
                              float2 *Q, float4 *partial, cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(calq32_kernel<TMA, MAXT, HLS, WS, A, MINB>,
+    cudaError_t e = cudaFuncSetAttribute(calq32_kernel<TMA, MAXT, HLS, WS, A, MINB, PAIR>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(calq32)");
     configured = true;
   }
-  calq32_kernel<TMA, MAXT, HLS, WS, A, MINB>
+  calq32_kernel<TMA, MAXT, HLS, WS, A, MINB, PAIR>
       <<<grid, threads, smem, st>>>(N, S, K2T, NST, NPL, C, GB, B32, fin, Q, partial);
   EDB_LAUNCHED();
   return EDB_OK;
@@ -776,31 +943,32 @@ static edb_status launch_c32_variant(int v, dim3 grid, int threads, size_t smem,
                                      int K2T, int NST, int NPL, int C, int GB, const float *B32,
                                      const float2 *fin, float2 *Q, float4 *partial,
                                      cudaStream_t st) {
+#define EDB_C32(MAXT, HLS, WS, A, MINB, PAIR)                                                   \
+  return launch_c32<TMA, MAXT, HLS, WS, A, MINB, PAIR>(grid, threads, smem, N, S, K2T, NST,    \
+                                                       NPL, C, GB, B32, fin, Q, partial, st)
   switch (v) {
-    case 1:
-      return launch_c32<TMA, 384, true, 8, 8, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C, GB, B32,
-                                                 fin, Q, partial, st);
-    case 2:
-      return launch_c32<TMA, 256, false, 2, 8, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C, GB,
-                                                  B32, fin, Q, partial, st);
-    case 3:
-      return launch_c32<TMA, 256, false, 8, 4, 2>(grid, threads, smem, N, S, K2T, NST, NPL, C, GB,
-                                                  B32, fin, Q, partial, st);
-    case 4:
-      return launch_c32<TMA, 384, false, 8, 4, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C, GB,
-                                                  B32, fin, Q, partial, st);
-    default:
-      return launch_c32<TMA, 256, false, 8, 8, 1>(grid, threads, smem, N, S, K2T, NST, NPL, C, GB,
-                                                  B32, fin, Q, partial, st);
+    case 1: EDB_C32(384, true, 8, 8, 1, false);
+    case 2: EDB_C32(256, false, 2, 8, 1, false);
+    case 3: EDB_C32(256, false, 8, 4, 2, false);
+    case 4: EDB_C32(384, false, 8, 4, 1, false);
+    case 5: EDB_C32(256, false, 8, 8, 1, true);
+    case 6: EDB_C32(384, true, 8, 8, 1, true);
+    case 7: EDB_C32(256, false, 2, 8, 1, true);
+    case 8: EDB_C32(256, false, 8, 4, 2, true);
+    case 9: EDB_C32(384, false, 8, 4, 1, true);
+    default: EDB_C32(256, false, 8, 8, 1, false);
   }
+#undef EDB_C32
 }
 
 edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin, float2 *d_Q,
-                               cudaStream_t st, int variant, int C, float4 *d_partial) {
+                               cudaStream_t st, int variant, int C, float4 *d_partial,
+                               float4 *d_pairs) {
   if (variant < 0 || variant >= calq32_variants()) variant = 0;
   if (C < 1 || C > N) return fail(EDB_EINVAL, "calq32: chunk count must be in [1, N]");
   if (C > 1 && !d_partial) return fail(EDB_EINVAL, "calq32: chunks need a partial-sum buffer");
   const C32Variant &vr = kC32Variants[variant];
+  if (vr.pair && !d_pairs) return fail(EDB_EINVAL, "calq32: pair variants need a pair buffer");
   const int maxt = vr.maxt, WS = vr.ws, A = vr.a;
   const int SG = SC * WS;
   const int R = (N + A - 1) / A;
@@ -813,8 +981,10 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   const int hlt = vr.hls ? threads : 0;
   // TMA bulk copies need 16-byte aligned sources: N % 4 == 0 makes every
   // row/line/plane offset a multiple of 16 bytes; the base pointers are checked
+  const float2 *src = vr.pair ? reinterpret_cast<const float2 *>(d_pairs) : d_fin;
+  const int units = vr.pair ? WS : SG, el = vr.pair ? 2 : 1;
   const bool tma = (N % 4) == 0 && N >= A && ((uintptr_t)d_B32 % 16) == 0 &&
-                   ((uintptr_t)d_fin % 16) == 0;
+                   ((uintptr_t)src % 16) == 0;
   // deepest pipeline that fits: two planes with >= 3 stages if possible,
   // else one plane with up to MAX_ST stages (the plain path uses 1 + 1)
   const size_t cap = vr.minb == 2 ? 113 * 1024 : 227 * 1024;
@@ -822,29 +992,35 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   if (tma) {
     NST = 0;
     for (int ns = MAX_ST; ns >= 3 && !NST; --ns)
-      if (c32_geom(N, A, K2T, ns, 2, hlt, SG).bytes <= cap) {
+      if (c32_geom(N, A, K2T, ns, 2, hlt, units, el).bytes <= cap) {
         NST = ns;
         NPL = 2;
       }
     for (int ns = MAX_ST; ns >= 2 && !NST; --ns)
-      if (c32_geom(N, A, K2T, ns, 1, hlt, SG).bytes <= cap) {
+      if (c32_geom(N, A, K2T, ns, 1, hlt, units, el).bytes <= cap) {
         NST = ns;
         NPL = 1;
       }
     if (!NST) return fail(EDB_EINVAL, "calq32: this variant does not fit in shared memory");
   }
-  const C32Geom g = c32_geom(N, A, K2T, NST, NPL, hlt, SG);
+  const C32Geom g = c32_geom(N, A, K2T, NST, NPL, hlt, units, el);
   if (g.bytes > cap) return fail(EDB_EINVAL, "calq32: this variant does not fit in shared memory");
   dim3 grid((unsigned)(((S + SG - 1) / SG) * C), (unsigned)N, (unsigned)tiles);
   // solve-group block of the CTA order: about 32 MB of f-hat kept in L2
   const long long group_bytes = (long long)SG * N * N * N * (long long)sizeof(float2);
   int GB = (int)std::max<long long>(1, (32LL << 20) / group_bytes) * C;
   if (GB > (int)grid.x) GB = (int)grid.x;
+  if (vr.pair) {
+    const long long n = (long long)((S + 1) / 2) * N * N * N;
+    const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+    c32_pairs_kernel<<<(unsigned)blocks, 256, 0, st>>>(S, (long long)N * N * N, d_fin, d_pairs);
+    EDB_LAUNCHED();
+  }
   edb_status rc =
       tma ? launch_c32_variant<true>(variant, grid, threads, g.bytes, N, S, K2T, NST, NPL, C, GB,
-                                     d_B32, d_fin, d_Q, d_partial, st)
+                                     d_B32, src, d_Q, d_partial, st)
           : launch_c32_variant<false>(variant, grid, threads, g.bytes, N, S, K2T, NST, NPL, C, GB,
-                                      d_B32, d_fin, d_Q, d_partial, st);
+                                      d_B32, src, d_Q, d_partial, st);
   if (rc != EDB_OK || C == 1) return rc;
   const long long n = (long long)S * N * N * N;
   const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);

@@ -24,6 +24,8 @@ def main():
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--sweep", action="store_true",
                     help="calq32: time every kernel variant (no chunks and 8 chunks)")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="calq32: run this kernel variant instead of the autotuned one")
     args = ap.parse_args()
 
     import torch
@@ -44,14 +46,20 @@ def main():
         if args.sweep:
             part = torch.empty(8 * S * N ** 3 * 4, dtype=torch.float32, device="cuda")
             nv = edb.lib.edb_qcalc_calQ_batch_f32_ex  # noqa: F841 (presence check)
+            nvar = edb.lib.edb_qcalc_batch_variants()
             for C in (1, 8):
-                for var in range(8):
+                first = None
+                for var in range(nvar):
                     try:
                         q.calQ_batch_f32_ex(S, var, C, part, fin, out, stream)
                     except edb.EdbError as e:
                         if e.status == 1 and var > 0:
                             continue
                         raise
+                    torch.cuda.synchronize()
+                    if first is None:
+                        first = out.clone()
+                    same = bool(torch.equal(out.view(torch.float32), first.view(torch.float32)))
                     a0 = torch.cuda.Event(enable_timing=True)
                     a1 = torch.cuda.Event(enable_timing=True)
                     a0.record(stream)
@@ -61,11 +69,16 @@ def main():
                     torch.cuda.synchronize()
                     t = a0.elapsed_time(a1) / args.reps
                     print(f"variant {var} chunks {C}: {t:.3f} ms, "
-                          f"{10 * float(N) ** 6 * S / (t * 1e-3) / 1e12:.2f} TFLOP/s")
+                          f"{10 * float(N) ** 6 * S / (t * 1e-3) / 1e12:.2f} TFLOP/s, "
+                          f"bits {'same' if same else 'DIFFER'}")
+                del first
             del part
-        v = q.autotune_batch(S, fin, out, stream)  # 3 launches per variant
-        print(f"autotuned variant {v}")
-        run = lambda: q.calQ_batch_f32(S, fin, out, stream)  # noqa: E731
+        if args.variant >= 0:
+            run = lambda: q.calQ_batch_f32_ex(S, args.variant, 1, None, fin, out, stream)  # noqa
+        else:
+            v = q.autotune_batch(S, fin, out, stream)  # 3 launches per variant
+            print(f"autotuned variant {v}")
+            run = lambda: q.calQ_batch_f32(S, fin, out, stream)  # noqa: E731
         terms = float(N) ** 6 * S
     else:
         q = edb.QCalculator(N, 0, L=args.L, filter=False, index_mode=args.mode)

@@ -143,15 +143,19 @@ edb_status edb_qcalc_calQ_batch_f32_device(edb_qcalc *q, int S, const float *d_f
 
 /* The batched kernel with an explicit variant and chunk count (no reference
  * counterpart; the autotuner and the serving engine choose these).
- * variant 0/1: 16-solve groups (CTA <= 256 threads with the compensated sums
- * in registers / <= 384 threads with them in shared memory); variant 2:
- * 4-solve groups.  chunks > 1 splits the l1 planes into that many chunks
- * whose compensated sums are added in order in FP64; d_partial (device)
- * then holds chunks x S x N^3 x 16 bytes.  For a given chunk count the result
- * of each solve does not depend on S or the variant. */
+ * variants 0-4: solves staged as they are; 0/1: 16-solve groups (CTA <= 256
+ * threads with the compensated sums in registers / <= 384 threads with them
+ * in shared memory); 2: 4-solve groups; 3/4: 4 outputs per thread (2 CTAs
+ * per SM / 384 threads).  Variants 5-9 are 0-4 on a solve-pair copy of the
+ * input, kept by the handle.  chunks > 1 splits the l1 planes into that many
+ * chunks whose compensated sums are added in order in FP64; d_partial
+ * (device) then holds chunks x S x N^3 x 16 bytes.  For a given chunk count
+ * the result of each solve does not depend on S or the variant. */
 edb_status edb_qcalc_calQ_batch_f32_ex(edb_qcalc *q, int S, int variant, int chunks,
                                        void *d_partial, const float *d_fin, float *d_Qout,
                                        void *stream);
+/* Number of batched-kernel variants (valid variant arguments are 0 .. n-1). */
+int edb_qcalc_batch_variants(void);
 
 /* FP64 collision sum that allocates nothing, for callers that may not call
  * cudaMalloc (a host that owns a fixed device pool and accounts for every

@@ -201,11 +201,12 @@ def test_batch_result_same_alone_and_in_the_mix(edb):
         assert torch.equal(one[0], mix[s])
 
 
-@pytest.mark.parametrize("N,L,chunks", [(8, 6.0, 4), (16, 6.0, 8), (24, 7.0, 8)])
+@pytest.mark.parametrize("N,L,chunks", [(8, 6.0, 4), (9, 6.0, 3), (16, 6.0, 8), (24, 7.0, 8)])
 def test_calQ_batch_variants_and_chunks(edb, oracle, N, L, chunks):
     """Every variant (16- and 4-solve groups, 8 or 4 outputs per thread,
-    registers / shared memory for the compensated sums) gives bit-identical
-    results for a given chunk count,
+    registers / shared memory for the compensated sums, plain or solve-pair
+    input layout; N = 9 takes the plain-load path) gives bit-identical
+    results for a given chunk count (S = 11: the last pair has one solve),
     a solve alone equals the same solve in a batch, and chunked and unchunked
     results meet the FP32 tolerance (relative L2 <= 5e-6) against the FP64
     oracle."""
@@ -219,7 +220,7 @@ def test_calQ_batch_variants_and_chunks(edb, oracle, N, L, chunks):
     part = torch.empty(chunks * S * N ** 3 * 4, dtype=torch.float32, device="cuda")
     res = {}
     for C in (1, chunks):
-        for v in range(8):
+        for v in range(edb.lib.edb_qcalc_batch_variants()):
             out = torch.empty_like(fin)
             try:
                 q.calQ_batch_f32_ex(S, v, C, part, fin, out)
@@ -231,10 +232,12 @@ def test_calQ_batch_variants_and_chunks(edb, oracle, N, L, chunks):
         for (c, v), r in res.items():
             if c == C:
                 assert np.array_equal(r, res[(C, 0)]), v
-        one = torch.empty_like(fin[3:4])
-        q.calQ_batch_f32_ex(1, 2, C, part, fin[3:4].contiguous(), one)
-        torch.cuda.synchronize()
-        assert np.array_equal(one.cpu().numpy()[0], res[(C, 0)][3])
+        assert len([k for k in res if k[0] == C]) >= 6
+        for v in (2, 7):
+            one = torch.empty_like(fin[3:4])
+            q.calQ_batch_f32_ex(1, v, C, part, fin[3:4].contiguous(), one)
+            torch.cuda.synchronize()
+            assert np.array_equal(one.cpu().numpy()[0], res[(C, 0)][3])
     Bo = oracle.genB(N, 0.0, L, False, INDEX_ALIASED)
     for s in (0, 7):
         Qo = oracle.calQ(N, Bo, fh[s], INDEX_ALIASED)
