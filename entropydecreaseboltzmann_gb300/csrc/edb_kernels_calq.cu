@@ -9,6 +9,8 @@
 //
 // Batched FP32 path (many solves sharing one B table, ALIASED mode): see the
 // comment above calq32_kernel.
+#include <cuda.h>
+
 #include <algorithm>
 
 #include "edb_internal.cuh"
@@ -206,6 +208,7 @@ constexpr int MAX_ST = 4;                 // pipeline stages (l-lines in flight)
 
 struct C32Geom {
   int N, A, R, RA, K2T, BROW, FLS, PSTR, NST, NPL, HLT, SG, EL;
+  int BSTG, FSTG;  // per-stage sizes: B tile (floats), f_l lines (float2)
   size_t off_B, off_fl, off_pl, off_hl, bytes;
 };
 
@@ -216,7 +219,7 @@ struct C32Geom {
 // solve pairs) of EL float2 per element (1: (re, im); 2: (re_a, re_b),
 // (im_a, im_b) of a pair).
 __host__ __device__ inline C32Geom c32_geom(int N, int A, int K2T, int NST, int NPL, int HLT,
-                                            int SG, int EL = 1) {
+                                            int SG, int EL, bool TMA) {
   C32Geom g;
   g.SG = SG;
   g.EL = EL;
@@ -228,7 +231,9 @@ __host__ __device__ inline C32Geom c32_geom(int N, int A, int K2T, int NST, int 
   g.NST = NST;
   g.NPL = NPL;
   g.HLT = HLT;
-  g.BROW = K2T * N + ROWPAD;
+  // TMA: tensor copies write dense boxes (B rows of K2T*N floats) to 128-byte
+  // aligned stage buffers
+  g.BROW = TMA ? K2T * N : K2T * N + ROWPAD;
   if (EL == 1) {
     g.FLS = g.RA + FLPAD;
     g.PSTR = N * N + PLPAD;
@@ -239,10 +244,16 @@ __host__ __device__ inline C32Geom c32_geom(int N, int A, int K2T, int NST, int 
     g.PSTR = (N * N + (9 - (N * N) % 8) % 8) * EL;
   }
   size_t o = 128;  // 2*MAX_ST + 2 mbarriers (+ pad)
+  g.BSTG = g.RA * g.BROW;
+  g.FSTG = SG * g.FLS;
+  if (TMA) {
+    g.BSTG = (g.BSTG + 31) / 32 * 32;
+    g.FSTG = (g.FSTG + 15) / 16 * 16;
+  }
   g.off_B = o;
-  o += sizeof(float) * (size_t)NST * g.RA * g.BROW;
+  o += sizeof(float) * (size_t)NST * g.BSTG;
   g.off_fl = o;
-  o += sizeof(float2) * (size_t)NST * SG * g.FLS;
+  o += sizeof(float2) * (size_t)NST * g.FSTG;
   g.off_pl = o;
   o += sizeof(float2) * (size_t)NPL * SG * g.PSTR;
   g.off_hl = o;
@@ -382,22 +393,55 @@ __device__ __forceinline__ void two_sum_fold2(u64 &hi, u64 &lo, u64 x) {
 }
 
 
-// Issue (TMA: warp 0, one copy per lane) or perform (plain: all threads) the
+// Tensor copies (one elected thread): the B tile of line li is one 5-D box
+// {k3: N, k2: K2T, k1: 1, l3: N, line: 1} of the table viewed as
+// [line][l3][k1][k2][k3]; the f_l lines of the group are one 3-D box
+// {FLS floats x 2, 1 line, SG units} of the input viewed as [unit][line][l3],
+// whose columns past N*EL complex are out of bounds and land as zeros.
+__device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *tm, int c0, int c1,
+                                            int c2, int c3, int c4, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(s_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4),
+      "r"(s_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, int c0, int c1,
+                                            int c2, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(s_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(c2), "r"(s_addr(bar))
+      : "memory");
+}
+
+// Issue (TMA: warp 0; tensor copies from one thread, or one bulk copy per B
+// row and f_l line from each lane) or perform (plain: all threads) the
 // staging of the B tile and f_l line of line li into buffer `st`.
 template <bool TMA>
 __device__ __forceinline__ void stage_line(const C32Geom &g, int li, int st, int k1, int k2_0,
                                            int k2n, int s0, int nval, long long NQ,
                                            const float *__restrict__ B32,
                                            const float2 *__restrict__ fin, float *Bs,
-                                           float2 *fls, uint64_t *full) {
+                                           float2 *fls, uint64_t *full, bool tmap,
+                                           const CUtensorMap *tmB, const CUtensorMap *tmF) {
   const int N = g.N;
-  float *Bd = Bs + (size_t)st * g.RA * g.BROW;
-  float2 *fd = fls + (size_t)st * g.SG * g.FLS;
+  float *Bd = Bs + (size_t)st * g.BSTG;
+  float2 *fd = fls + (size_t)st * g.FSTG;
   const float *Bsrc = B32 + (long long)li * N * NQ + (long long)k1 * N * N + (long long)k2_0 * N;
   const int EL = g.EL;  // s0 / nval count data units of EL float2 per element
   const float2 *fsrc = fin + ((long long)s0 * NQ + (long long)li * N) * EL;
   const int rowlen = k2n * N;
-  if (TMA) {  // called by warp 0 only
+  if (TMA && tmap) {  // called by warp 0 only
+    if ((threadIdx.x & 31) == 0) {
+      mbar_expect_tx(full + st, (uint32_t)(N * g.K2T * N * 4 + g.SG * g.FLS * 8));
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      tma_load_5d(Bd, tmB, 0, k2_0, k1, 0, li, full + st);
+      tma_load_3d(fd, tmF, 0, li, s0, full + st);
+    }
+    __syncwarp();
+  } else if (TMA) {  // called by warp 0 only
     const int lane = threadIdx.x & 31;
     if (lane == 0) mbar_expect_tx(full + st, (uint32_t)(N * rowlen * 4 + nval * N * 8 * EL));
     __syncwarp();
@@ -616,11 +660,13 @@ template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB, bool PAIR>
 __global__ void __launch_bounds__(MAXT, MINB)
     calq32_kernel(int N, int S, int K2T, int NST, int NPL, int C, int GB,
                   const float *__restrict__ B32, const float2 *__restrict__ fin,
-                  float2 *__restrict__ Q, float4 *__restrict__ partial) {
+                  float2 *__restrict__ Q, float4 *__restrict__ partial, int tmap,
+                  const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmF) {
   constexpr int SG = SC * WS;  // solves per group
   extern __shared__ __align__(128) unsigned char smem[];
   const C32Geom g =
-      c32_geom(N, A, K2T, NST, NPL, HLS ? (int)blockDim.x : 0, PAIR ? WS : SG, PAIR ? 2 : 1);
+      c32_geom(N, A, K2T, NST, NPL, HLS ? (int)blockDim.x : 0, PAIR ? WS : SG, PAIR ? 2 : 1,
+               TMA && tmap);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);  // [MAX_ST]
   uint64_t *empty = full + MAX_ST;                       // [MAX_ST]
   uint64_t *pbar = full + 2 * MAX_ST;                    // [2] planes
@@ -706,7 +752,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
   int issued = 0, planes = 0;  // counted in warp 0
   if (TMA && warp == 0 && nlines > 0) {
     for (int j = 0; j < NST - 1 && j < nlines; ++j, ++issued)
-      stage_line<true>(g, li0 + j, j % NST, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full);
+      stage_line<true>(g, li0 + j, j % NST, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full, tmap, &tmB, &tmF);
     stage_plane<true>(g, (k1 - P0 + N) % N, u0, nval, NQ, fin, plb, &pbar[0]);
     ++planes;
   }
@@ -749,20 +795,20 @@ __global__ void __launch_bounds__(MAXT, MINB)
       if (warp == 0 && jn < nlines) {
         const int sn = jn % NST;
         if (j >= 1) mbar_wait(&empty[sn], (uint32_t)(((j - 1) / NST) & 1), to);
-        stage_line<true>(g, li0 + jn, sn, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full);
+        stage_line<true>(g, li0 + jn, sn, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full, tmap, &tmB, &tmF);
         ++issued;
       }
       mbar_wait(&full[st], (uint32_t)((j / NST) & 1), to);
     } else {
       __syncthreads();  // previous line's readers are done (single buffer)
-      stage_line<false>(g, li, st, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full);
+      stage_line<false>(g, li, st, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full, tmap, &tmB, &tmF);
       __syncthreads();
     }
 
     // ---- compute line (l1, l2)
     const int m2 = (k2c - l2 + N) % N;
-    const float *Bt = Bs + (size_t)st * g.RA * g.BROW + k2l * N + k3_0;
-    const float2 *fl0 = fls + (size_t)st * g.SG * g.FLS + (size_t)w * g.FLS;
+    const float *Bt = Bs + (size_t)st * g.BSTG + k2l * N + k3_0;
+    const float2 *fl0 = fls + (size_t)st * g.FSTG + (size_t)w * g.FLS;
     const float2 *p0 = plb + (size_t)pb * plane_sz + (size_t)w * g.PSTR + m2 * N * g.EL;
     if (PAIR) {
       if (TMA)
@@ -921,10 +967,45 @@ int calq32_group(int variant) { return SC * kC32Variants[variant].ws; }
 bool calq32_pair(int variant) { return kC32Variants[variant].pair; }
 size_t calq32_pair_bytes(int N, int S) { return (size_t)((S + 1) / 2) * N * N * N * sizeof(float4); }
 
+// Tensor maps of one launch (tmap = 0: bulk copies, the maps are unused).
+struct C32Maps {
+  int tmap = 0;
+  CUtensorMap B, F;
+};
+
+// cuTensorMapEncodeTiled from the driver (through the runtime's entry-point
+// query, so the library links no driver stub).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static const EncodeTiledFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+// FP32 tiled map, no swizzle, out-of-bounds elements read as zero.
+static bool encode_map(CUtensorMap *m, int rank, const void *base, const cuuint64_t *dim,
+                       const cuuint64_t *stride, const cuuint32_t *box) {
+  const EncodeTiledFn fn = encode_tiled();
+  if (!fn) return false;
+  const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank, const_cast<void *>(base), dim,
+            stride, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB, bool PAIR>
 static edb_status launch_c32(dim3 grid, int threads, size_t smem, int N, int S, int K2T, int NST,
                              int NPL, int C, int GB, const float *B32, const float2 *fin,
-                             float2 *Q, float4 *partial, cudaStream_t st) {
+                             float2 *Q, float4 *partial, const C32Maps &maps, cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(calq32_kernel<TMA, MAXT, HLS, WS, A, MINB, PAIR>,
@@ -933,7 +1014,8 @@ static edb_status launch_c32(dim3 grid, int threads, size_t smem, int N, int S, 
     configured = true;
   }
   calq32_kernel<TMA, MAXT, HLS, WS, A, MINB, PAIR>
-      <<<grid, threads, smem, st>>>(N, S, K2T, NST, NPL, C, GB, B32, fin, Q, partial);
+      <<<grid, threads, smem, st>>>(N, S, K2T, NST, NPL, C, GB, B32, fin, Q, partial, maps.tmap,
+                                    maps.B, maps.F);
   EDB_LAUNCHED();
   return EDB_OK;
 }
@@ -942,10 +1024,11 @@ template <bool TMA>
 static edb_status launch_c32_variant(int v, dim3 grid, int threads, size_t smem, int N, int S,
                                      int K2T, int NST, int NPL, int C, int GB, const float *B32,
                                      const float2 *fin, float2 *Q, float4 *partial,
-                                     cudaStream_t st) {
+                                     const C32Maps &maps, cudaStream_t st) {
 #define EDB_C32(MAXT, HLS, WS, A, MINB, PAIR)                                                   \
   return launch_c32<TMA, MAXT, HLS, WS, A, MINB, PAIR>(grid, threads, smem, N, S, K2T, NST,    \
-                                                       NPL, C, GB, B32, fin, Q, partial, st)
+                                                       NPL, C, GB, B32, fin, Q, partial, maps, \
+                                                       st)
   switch (v) {
     case 1: EDB_C32(384, true, 8, 8, 1, false);
     case 2: EDB_C32(256, false, 2, 8, 1, false);
@@ -985,6 +1068,25 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   const int units = vr.pair ? WS : SG, el = vr.pair ? 2 : 1;
   const bool tma = (N % 4) == 0 && N >= A && ((uintptr_t)d_B32 % 16) == 0 &&
                    ((uintptr_t)src % 16) == 0;
+  // line staging by two tensor copies when the f_l box fits (<= 256 floats a
+  // row), else by one bulk copy per B row and f_l line
+  C32Maps maps;
+  if (tma && 2 * c32_geom(N, A, K2T, 1, 1, 0, units, el, true).FLS <= 256 && N <= 256) {
+    const int FLS = c32_geom(N, A, K2T, 1, 1, 0, units, el, true).FLS;
+    const long long NQ = (long long)N * N * N;
+    const cuuint64_t bdim[5] = {(cuuint64_t)N, (cuuint64_t)N, (cuuint64_t)N, (cuuint64_t)N,
+                                (cuuint64_t)N * N};
+    const cuuint64_t bstr[4] = {(cuuint64_t)N * 4, (cuuint64_t)N * N * 4, (cuuint64_t)NQ * 4,
+                                (cuuint64_t)N * NQ * 4};
+    const cuuint32_t bbox[5] = {(cuuint32_t)N, (cuuint32_t)K2T, 1, (cuuint32_t)N, 1};
+    const long long nunits = vr.pair ? (S + 1) / 2 : S;
+    const cuuint64_t fdim[3] = {(cuuint64_t)N * 2 * el, (cuuint64_t)N * N, (cuuint64_t)nunits};
+    const cuuint64_t fstr[2] = {(cuuint64_t)N * 8 * el, (cuuint64_t)NQ * 8 * el};
+    const cuuint32_t fbox[3] = {(cuuint32_t)(2 * FLS), 1, (cuuint32_t)units};
+    if (encode_map(&maps.B, 5, d_B32, bdim, bstr, bbox) &&
+        encode_map(&maps.F, 3, src, fdim, fstr, fbox))
+      maps.tmap = 1;
+  }
   // deepest pipeline that fits: two planes with >= 3 stages if possible,
   // else one plane with up to MAX_ST stages (the plain path uses 1 + 1)
   const size_t cap = vr.minb == 2 ? 113 * 1024 : 227 * 1024;
@@ -992,18 +1094,18 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   if (tma) {
     NST = 0;
     for (int ns = MAX_ST; ns >= 3 && !NST; --ns)
-      if (c32_geom(N, A, K2T, ns, 2, hlt, units, el).bytes <= cap) {
+      if (c32_geom(N, A, K2T, ns, 2, hlt, units, el, maps.tmap).bytes <= cap) {
         NST = ns;
         NPL = 2;
       }
     for (int ns = MAX_ST; ns >= 2 && !NST; --ns)
-      if (c32_geom(N, A, K2T, ns, 1, hlt, units, el).bytes <= cap) {
+      if (c32_geom(N, A, K2T, ns, 1, hlt, units, el, maps.tmap).bytes <= cap) {
         NST = ns;
         NPL = 1;
       }
     if (!NST) return fail(EDB_EINVAL, "calq32: this variant does not fit in shared memory");
   }
-  const C32Geom g = c32_geom(N, A, K2T, NST, NPL, hlt, units, el);
+  const C32Geom g = c32_geom(N, A, K2T, NST, NPL, hlt, units, el, maps.tmap);
   if (g.bytes > cap) return fail(EDB_EINVAL, "calq32: this variant does not fit in shared memory");
   dim3 grid((unsigned)(((S + SG - 1) / SG) * C), (unsigned)N, (unsigned)tiles);
   // solve-group block of the CTA order: about 32 MB of f-hat kept in L2
@@ -1018,9 +1120,9 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   }
   edb_status rc =
       tma ? launch_c32_variant<true>(variant, grid, threads, g.bytes, N, S, K2T, NST, NPL, C, GB,
-                                     d_B32, src, d_Q, d_partial, st)
+                                     d_B32, src, d_Q, d_partial, maps, st)
           : launch_c32_variant<false>(variant, grid, threads, g.bytes, N, S, K2T, NST, NPL, C, GB,
-                                      d_B32, src, d_Q, d_partial, st);
+                                      d_B32, src, d_Q, d_partial, maps, st);
   if (rc != EDB_OK || C == 1) return rc;
   const long long n = (long long)S * N * N * N;
   const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
