@@ -285,6 +285,11 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
       "l"(src), "r"(bytes), "r"(s_addr(bar))
       : "memory");
 }
+// Lanes of the calling warp that exist (the last warp of a CTA may be partial).
+__device__ __forceinline__ unsigned warp_mask() {
+  const int wl = min(32, (int)blockDim.x - (int)(threadIdx.x & ~31u));
+  return wl == 32 ? 0xffffffffu : ((1u << wl) - 1u);
+}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -440,11 +445,11 @@ __device__ __forceinline__ void stage_line(const C32Geom &g, int li, int st, int
       tma_load_5d(Bd, tmB, 0, k2_0, k1, 0, li, full + st);
       tma_load_3d(fd, tmF, 0, li, s0, full + st);
     }
-    __syncwarp();
+    __syncwarp(warp_mask());
   } else if (TMA) {  // called by warp 0 only
     const int lane = threadIdx.x & 31;
     if (lane == 0) mbar_expect_tx(full + st, (uint32_t)(N * rowlen * 4 + nval * N * 8 * EL));
-    __syncwarp();
+    __syncwarp(warp_mask());
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     for (int l3 = lane; l3 < N; l3 += 32)
       bulk_g2s(Bd + (size_t)l3 * g.BROW, Bsrc + (long long)l3 * NQ, rowlen * 4, full + st);
@@ -471,7 +476,7 @@ __device__ __forceinline__ void stage_plane(const C32Geom &g, int m1, int s0, in
   if (TMA) {  // warp 0 only
     const int lane = threadIdx.x & 31;
     if (lane == 0) mbar_expect_tx(bar, (uint32_t)(nval * NN * 8 * EL));
-    __syncwarp();
+    __syncwarp(warp_mask());
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     for (int s = lane; s < nval; s += 32)
       bulk_g2s(pl + (size_t)s * g.PSTR, src + (long long)s * NQ * EL, NN * 8 * EL, bar);
@@ -824,7 +829,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
         compute_line<false, false, A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
     }
     if (TMA) {
-      __syncwarp();
+      __syncwarp(warp_mask());
       if (lane == 0) mbar_arrive(&empty[st]);
     }
     if ((l2 + 1) % FOLD_LINES == 0 || l2 == N - 1) {  // fold into the compensated pair
