@@ -709,11 +709,19 @@ __global__ void __launch_bounds__(MAXT, MINB)
   // staged data units (solves, or solve pairs) of this group
   const int u0 = PAIR ? s0 / 2 : s0;
   const int nval = PAIR ? min(WS, (S - s0 + 1) / 2) : min(SG, S - s0);
-  // this chunk's l1 planes [P0, P1) and l-lines [li0, li0 + nlines)
-  const int PPC = (N + C - 1) / C;
-  const int P0 = min(N, chunk * PPC), P1 = min(N, P0 + PPC);
+  // The table is the symmetric pair table (see genB_kernel): only the l1
+  // planes with l1 <= m1 = (k1 - l1) mod N are visited, in increasing l1:
+  // [0, k1 / 2] and [k1 + 1, (k1 + N) / 2].  Plane p of that list is
+  // l1 = plane_l1(p).  This chunk takes list entries [P0, P1) and walks their
+  // l-lines j = 0 .. nlines - 1 (line j: plane P0 + j / N, l2 = j mod N).
+  const int plo = k1 / 2;
+  const int nlist = plo + 1 + max(0, (k1 + N) / 2 - k1);
+  auto plane_l1 = [&](int p) { return p <= plo ? p : k1 + 1 + (p - plo - 1); };
+  const int PPC = (nlist + C - 1) / C;
+  const int P0 = min(nlist, chunk * PPC), P1 = min(nlist, P0 + PPC);
   const int nplanes = P1 - P0;
-  const int li0 = P0 * N, nlines = nplanes * N;
+  const int nlines = nplanes * N;
+  auto line_li = [&](int j) { return plane_l1(P0 + j / N) * N + j % N; };
   const size_t plane_sz = (size_t)g.SG * g.PSTR;
 
   // zero the tile/line buffers once: padded rows (l3 >= N), row tails and the
@@ -757,16 +765,17 @@ __global__ void __launch_bounds__(MAXT, MINB)
   int issued = 0, planes = 0;  // counted in warp 0
   if (TMA && warp == 0 && nlines > 0) {
     for (int j = 0; j < NST - 1 && j < nlines; ++j, ++issued)
-      stage_line<true>(g, li0 + j, j % NST, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full, tmap, &tmB, &tmF);
-    stage_plane<true>(g, (k1 - P0 + N) % N, u0, nval, NQ, fin, plb, &pbar[0]);
+      stage_line<true>(g, line_li(j), j % NST, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls,
+                       full, tmap, &tmB, &tmF);
+    stage_plane<true>(g, (k1 - plane_l1(P0) + N) % N, u0, nval, NQ, fin, plb, &pbar[0]);
     ++planes;
   }
   bool to = false;
   bool aborted = false;
   for (int j = 0; j < nlines; ++j) {
-    const int li = li0 + j;
+    const int li = line_li(j);
     const int l1 = li / N, l2 = li % N;
-    const int pr = l1 - P0;
+    const int pr = j / N;  // plane within the chunk
     const int st = j % NST;
     const int pb = (NPL == 2) ? (pr & 1) : 0;
     if (l2 == 0) {
@@ -778,7 +787,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
       if (TMA) {
         if (NPL == 2) {
           if (warp == 0 && pr + 1 < nplanes) {
-            stage_plane<true>(g, (k1 - (l1 + 1) + N) % N, u0, nval, NQ, fin,
+            stage_plane<true>(g, (k1 - plane_l1(P0 + pr + 1) + N) % N, u0, nval, NQ, fin,
                               plb + (size_t)((pr + 1) & 1) * plane_sz, &pbar[(pr + 1) & 1]);
             ++planes;
           }
@@ -800,7 +809,8 @@ __global__ void __launch_bounds__(MAXT, MINB)
       if (warp == 0 && jn < nlines) {
         const int sn = jn % NST;
         if (j >= 1) mbar_wait(&empty[sn], (uint32_t)(((j - 1) / NST) & 1), to);
-        stage_line<true>(g, li0 + jn, sn, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full, tmap, &tmB, &tmF);
+        stage_line<true>(g, line_li(jn), sn, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full,
+                         tmap, &tmB, &tmF);
         ++issued;
       }
       mbar_wait(&full[st], (uint32_t)((j / NST) & 1), to);

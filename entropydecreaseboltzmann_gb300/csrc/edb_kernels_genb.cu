@@ -217,8 +217,15 @@ edb_status launch_bmm(int N, double gamma, double L, int filter, int mode, const
 }
 
 // One CTA per row l (centred); columns k over all N^3 centred modes.
-// Writes B64[l][k] (when given) and, when B32 is given, the same value as
-// float at the FFTW-order position [lf][kf] (lf = (l - n) mod N per dimension).
+// Writes B64[l][k] (when given) and, when B32 is given, the symmetric pair
+// table of the batched kernel at the FFTW-order position [lf][kf]
+// (lf = (l - n) mod N per dimension): the terms l and m = k - l of a Q-hat sum
+// carry the same product f_l f_m, so the batched kernel visits only the l1
+// planes with l1 <= m1 and weights them by B[l][k] + B[m][k], computed here in
+// FP64 and rounded once; on the planes l1 = m1 (both terms inside the plane)
+// the entry stays B[l][k].  The partner's value needs no second table lookup:
+// l + m and |l - m| are the same for both, so B[m][k] differs from B[l][k]
+// only in its self-interaction term, Bmm[l] instead of Bmm[m].
 __global__ void genB_kernel(int N, int filter, double rval, const double *__restrict__ T, int amax,
                             const double *__restrict__ sigma, const double *__restrict__ Bmm,
                             double *__restrict__ B64, float *__restrict__ B32) {
@@ -246,11 +253,14 @@ __global__ void genB_kernel(int N, int filter, double rval, const double *__rest
     int b = e1 * e1 + e2 * e2 + e3 * e3;
     double sigmam = filter ? sigma[m1] * sigma[m2] * sigma[m3] : 1.0;
     long long m = ((long long)m1 * N + m2) * N + m3;
-    double v = T[(long long)a * W + b] * sigmal * sigmam * rval - Bmm[m];
+    const double t = T[(long long)a * W + b];
+    double v = t * sigmal * sigmam * rval - Bmm[m];
     if (B64) B64[lc * NQ + kc] = v;
     if (B32) {
       long long kf = ((long long)((k1 - n + N) % N) * N + (k2 - n + N) % N) * N + (k3 - n + N) % N;
-      B32[lf * NQ + kf] = (float)v;
+      double w = v;
+      if (l1 != m1) w += t * sigmam * sigmal * rval - Bmm[lc];  // B[m][k], as its row writes it
+      B32[lf * NQ + kf] = (float)w;
     }
   }
 }
