@@ -301,6 +301,9 @@ def main():
     torch.cuda.synchronize()
     k_ms = k0.elapsed_time(k1) / kreps
     terms = float(NQ) * NQ * S
+    # l1 planes visited per k1: [0, k1/2] and [k1+1, (k1+N)/2]
+    executed_terms = float(S) * N ** 4 * sum(
+        k1 // 2 + 1 + max(0, (k1 + N) // 2 - k1) for k1 in range(N))
     algo_bytes = 4.0 * NQ * NQ + S * NQ * (8 + 8)  # B32 once, FP32 f-hat in, FP32 Q-hat out
     peak_tf = C_double_peak(edb)
     achieved_tf = 10.0 * terms / (k_ms * 1e-3) / 1e12
@@ -391,7 +394,7 @@ def main():
             "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf,
                          "unit": "TFLOP/s", "frac": achieved_tf / peak_tf,
                          # dram__bytes_read.sum + dram__bytes_write.sum per launch, one ncu
-                         # capture of this launch (N=24, S=4096, the autotuned variant 3)
+                         # capture of this launch (N=24, S=4096, the autotuned variant)
                          "traffic": TRAFFIC_BYTES if S == S_BATCH else None,
                          "traffic_note": "bytes per launch from ncu; algorithmic bytes are "
                                          f"{algo_bytes / 1e9:.2f} GB (table once + f-hat in, "
@@ -399,6 +402,11 @@ def main():
                                          "solve groups, and the kernel is FP32-bound",
                          "kernel": "calq32_kernel", "ms_per_launch": k_ms,
                          "flop_per_launch": 10.0 * terms,
+                         # the kernel sums each symmetric pair of terms (l, k - l) once:
+                         # the pair terms it executes, and their rate on the FP32 pipe
+                         "executed_terms_per_launch": executed_terms,
+                         "executed_tflops": 10.0 * executed_terms / (k_ms * 1e-3) / 1e12,
+                         "executed_frac": 10.0 * executed_terms / (k_ms * 1e-3) / 1e12 / peak_tf,
                          "peak_source": "FP32 FMA probe measured in this run (edb_measure_fp32_peak)"},
             "fp64_dropin": fp64, "hbm_peak_GBs": peaks["hbm_gbs"], "hbm_peak_source": peak_src,
             # the plain FP64 single-solve path (native FP64 arithmetic) and the

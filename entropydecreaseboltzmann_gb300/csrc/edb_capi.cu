@@ -188,6 +188,14 @@ static int amax_of(int N) {
   return 3 * hi * hi;
 }
 
+// The double-float kernel's table: in ALIASED mode the symmetric pair table
+// (half the l1 planes are visited), else B split as it is.
+static bool qcalc_b2_paired(const edb_qcalc *q) { return q->p.mode == EDB_INDEX_ALIASED; }
+static edb_status qcalc_split_B2(edb_qcalc *q) {
+  if (qcalc_b2_paired(q)) return launch_split_B_paired(q->p.N, q->B64, q->B2, q->st);
+  return launch_split_B(q->p.NQ * q->p.NQ, q->B64, q->B2, q->st);
+}
+
 static edb_status qcalc_alloc_work(edb_qcalc *q) {
   if (!q->partial) {
     q->nchunk = calq64_nchunk(q->p);
@@ -217,10 +225,10 @@ static edb_status qcalc_tune_fp64(edb_qcalc *q) {
   int best_minb = 2;
   edb_status rc = EDB_OK;
   for (int minb = 2; minb >= 1 && rc == EDB_OK; --minb) {
-    rc = launch_calq64x(q->p, q->B2, q->fdf, q->partial, q->Q, st, minb);
+    rc = launch_calq64x(q->p, q->B2, q->fdf, q->partial, q->Q, st, minb, qcalc_b2_paired(q));
     cudaEventRecord(e0, st);
     for (int r = 0; r < 2 && rc == EDB_OK; ++r)
-      rc = launch_calq64x(q->p, q->B2, q->fdf, q->partial, q->Q, st, minb);
+      rc = launch_calq64x(q->p, q->B2, q->fdf, q->partial, q->Q, st, minb, qcalc_b2_paired(q));
     cudaEventRecord(e1, st);
     cudaError_t ce = cudaEventSynchronize(e1);
     if (ce != cudaSuccess) {
@@ -262,7 +270,7 @@ extern "C" edb_status edb_qcalc_genB(edb_qcalc *q) {
   if (s == EDB_OK)
     s = launch_genB(N, q->d.gamma, q->d.L, q->d.filter, q->d.index_mode, T, amax, sigma, Bmm,
                     q->B64, q->B32, q->st);
-  if (s == EDB_OK) s = launch_split_B(NQ * NQ, q->B64, q->B2, q->st);
+  if (s == EDB_OK) s = qcalc_split_B2(q);
   cudaError_t e = cudaStreamSynchronize(q->st);
   dfree(T);
   dfree(sigma);
@@ -365,7 +373,7 @@ extern "C" edb_status edb_qcalc_set_B(edb_qcalc *q, const double *host_B) {
   EDB_TRY(qcalc_alloc_work(q));
   EDB_CUDA(cudaMemcpy(q->B64, host_B, sizeof(double) * NQ * NQ, cudaMemcpyHostToDevice));
   if (!q->B2) EDB_TRY(dalloc(&q->B2, (size_t)NQ * NQ));
-  EDB_TRY(launch_split_B(NQ * NQ, q->B64, q->B2, q->st));
+  EDB_TRY(qcalc_split_B2(q));
   EDB_CUDA(cudaStreamSynchronize(q->st));
   dfree(q->B32);  // the FP32 copy no longer matches
   q->ready = true;
@@ -398,7 +406,8 @@ extern "C" edb_status edb_qcalc_get_info(edb_qcalc *q, edb_qcalc_info *out) {
 static edb_status qcalc_fp64(edb_qcalc *q, const double2 *in, double2 *out, cudaStream_t st) {
   if (q->fp64_kernel == EDB_FP64_EMULATED && q->B2) {
     EDB_TRY(launch_split_f(q->p.NQ, in, q->fdf, st));
-    return launch_calq64x(q->p, q->B2, q->fdf, q->partial, out, st, q->c64x_minb);
+    return launch_calq64x(q->p, q->B2, q->fdf, q->partial, out, st, q->c64x_minb,
+                          qcalc_b2_paired(q));
   }
   return launch_calq64(q->p, q->B64, in, q->partial, out, st);
 }

@@ -108,11 +108,17 @@ edb_status launch_calq64_reduce(const QParams &p, int nchunk, const double2 *d_p
 int calq64x_nchunk(const QParams &p, int *J2T_out);
 edb_status launch_split_f(long long n, const double2 *f, float4 *out, cudaStream_t st);
 edb_status launch_split_B(long long n, const double *B, float2 *B2, cudaStream_t st);
-// minb selects the register cap (2: 128 registers, 1: up to 255).
+// ALIASED tables: B2 = split of the symmetric pair table (B[l][k] + B[k-l][k]
+// off the planes l1 = m1), read by launch_calq64x with paired = true.
+edb_status launch_split_B_paired(int N, const double *B, float2 *B2, cudaStream_t st);
+// minb selects the register cap (2: 128 registers, 1: up to 255).  paired:
+// B2 is the pair table and only the l1 planes with l1 <= m1 are visited.
 edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const float4 *d_fdf,
-                          double2 *d_partial, double2 *d_Q, cudaStream_t st, int minb);
+                          double2 *d_partial, double2 *d_Q, cudaStream_t st, int minb,
+                          bool paired);
 
-// Batched FP32 calQ (ALIASED): S solves, B32 in FFTW order.
+// Batched FP32 calQ (ALIASED): S solves, B32 the symmetric pair table in FFTW
+// order (see genB_kernel).
 // variant in [0, calq32_variants()) selects the solve group and CTA shape
 // (see the kernel).  C > 1 splits the l1 planes into C chunks reduced in
 // order in FP64; d_partial then holds C * S * N^3 float4.  Pair variants

@@ -170,6 +170,26 @@ __global__ void b2_split_kernel(long long n, const double *__restrict__ B, float
   B2[i] = make_float2(h, (float)(v - (double)h));
 }
 
+// The paired table of the double-float kernel (ALIASED, P = N): entry
+// [l][k] (centred) is B[l][k] + B[m][k], m the partner row with
+// m_d = (k_d - l_d + n) mod N, summed in FP64 and then split, or B[l][k]
+// alone when l and m share the first index (both terms lie on one visited
+// plane).  The terms l and m of a Q-hat sum carry the same product f_l f_m.
+__global__ void b2_pair_split_kernel(int N, const double *__restrict__ B, float2 *__restrict__ B2) {
+  const long long NQ = (long long)N * N * N;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NQ * NQ) return;
+  const long long l = i / NQ, k = i - l * NQ;
+  const int n = (N - 1) / 2;
+  const int l1 = (int)(l / (N * N)), l2 = (int)((l / N) % N), l3 = (int)(l % N);
+  const int k1 = (int)(k / (N * N)), k2 = (int)((k / N) % N), k3 = (int)(k % N);
+  const int m1 = (k1 - l1 + n + N) % N, m2 = (k2 - l2 + n + N) % N, m3 = (k3 - l3 + n + N) % N;
+  double v = B[i];
+  if (m1 != l1) v += B[(((long long)m1 * N + m2) * N + m3) * NQ + k];
+  const float h = (float)v;
+  B2[i] = make_float2(h, (float)(v - (double)h));
+}
+
 // TMA: per-warp bulk-copy ring for B (requires contiguous, aligned warp
 // segments; see the launcher).  Otherwise __ldg one row ahead.
 // MINB: minimum resident CTAs per SM the register allocation must allow
@@ -177,7 +197,7 @@ __global__ void b2_split_kernel(long long n, const double *__restrict__ B, float
 // timing both (edb_qcalc_genB runs the comparison once per table).
 template <bool TMA, int MINB>
 __global__ void __launch_bounds__(256, MINB)
-    calq64x_kernel(QParams p, int J2T, int LC, const float2 *__restrict__ B2,
+    calq64x_kernel(QParams p, int J2T, int LC, int paired, const float2 *__restrict__ B2,
                    const float4 *__restrict__ fdf, double2 *__restrict__ partial) {
   extern __shared__ __align__(128) unsigned char smem64[];
   const int N = p.N, P = p.P;
@@ -202,8 +222,25 @@ __global__ void __launch_bounds__(256, MINB)
   const int j2c = ok ? j2 : 0;
   const int j3_0 = r * RUN;
   const int chunk = blockIdx.z;
-  const int NL = N * N;
-  const int c0 = chunk * LC, c1 = min(NL, c0 + LC);
+  // l1 planes this output plane visits.  Paired table (ALIASED): the terms l
+  // and m = k - l share the product f_l f_m and B2 holds B[l][k] + B[m][k], so
+  // only the planes with a1 <= (k1 - a1) mod N are visited (a1, k1 in FFTW
+  // order): [0, k1/2] and [k1+1, (k1+N)/2].  Otherwise every i1 in order.
+  const int k1f = (j1 - p.n + N) % N;
+  const int plo = k1f / 2;
+  const int nlist = paired ? plo + 1 + max(0, (k1f + N) / 2 - k1f) : N;
+  auto plane_i1 = [&](int pi) {
+    if (!paired) return pi;
+    const int a = pi <= plo ? pi : k1f + 1 + (pi - plo - 1);
+    return (a + p.n) % N;  // a = (i1 - n) mod N
+  };
+  const int NL = nlist * N;  // l-lines (i1, i2) of those planes
+  const int c0 = min(NL, chunk * LC), c1 = min(NL, c0 + LC);
+  // B2 row of the chunk's qq-th row (line c0 + qq / N, i3 = qq mod N)
+  auto row_of = [&](int qq) -> long long {
+    const int t = c0 + qq / N;
+    return ((long long)plane_i1(t / N) * N + t % N) * N + qq % N;
+  };
   const long long kcol = ((long long)j1 * P + j2c) * P + j3_0;
   // columns past P (ragged last run) read a clamped, in-row column and are
   // masked out of the output
@@ -218,6 +255,17 @@ __global__ void __launch_bounds__(256, MINB)
   const uint32_t seg_bytes = (uint32_t)(wthreads * RUN * sizeof(float2));
   const int nrows = (c1 - c0) * N;  // rows this CTA streams
   bool to = false;
+  // refill cursor (lane 0): row q + DEPTH of the chunk as (list plane, i2, i3),
+  // advanced by one row per refill so the per-row path has no division
+  int rf_pi = 0, rf_i2 = 0, rf_i3 = 0;
+  long long rf_base = 0;
+  if (TMA && lane == 0 && DEPTH < nrows) {
+    const int t = c0 + DEPTH / N;
+    rf_pi = t / N;
+    rf_i2 = t % N;
+    rf_i3 = DEPTH % N;
+    rf_base = ((long long)plane_i1(rf_pi) * N + rf_i2) * N;
+  }
 
   if (TMA) {
     if (lane == 0) {
@@ -227,7 +275,7 @@ __global__ void __launch_bounds__(256, MINB)
     __syncwarp();
     if (lane == 0) {  // prologue: the first DEPTH rows
       for (int q = 0; q < DEPTH && q < nrows; ++q) {
-        const long long lflat = (long long)c0 * N + q;  // rows of the chunk are consecutive
+        const long long lflat = row_of(q);
         mbar_expect_tx(&mybar[q], seg_bytes);
         bulk_g2s(myring + (size_t)q * 32 * RUN, B2 + lflat * p.KC + wcol, seg_bytes, &mybar[q]);
       }
@@ -245,12 +293,12 @@ __global__ void __launch_bounds__(256, MINB)
   const int fi0 = p.sL % N;             // f_l entry at i3 = 0
   int cur_i1 = -1;
   int q = 0;  // row counter within the chunk
-  // running line indices: i1, i2 of the line; a1, a2 = (i + sL) mod N;
-  // m2 = (j2 - i2 + sM) mod N
-  int i1 = c0 / N, i2 = c0 % N;
-  int a1 = (i1 + p.sL) % N, a2 = (i2 + p.sL) % N;
-  int m2 = ((j2c - i2 + p.sM) % N + N) % N;
   for (int line = c0; line < c1; ++line) {
+    // line indices: i1, i2 (centred l); a1, a2 = (i + sL) mod N (f_l, FFTW
+    // order); m2 = (j2 - i2 + sM) mod N
+    const int i1 = plane_i1(line / N), i2 = line % N;
+    const int a1 = (i1 + p.sL) % N, a2 = (i2 + p.sL) % N;
+    const int m2 = ((j2c - i2 + p.sM) % N + N) % N;
     if (i1 != cur_i1) {  // stage the m1-plane
       cur_i1 = i1;
       const int m1 = ((j1 - i1 + p.sM) % N + N) % N;
@@ -260,7 +308,7 @@ __global__ void __launch_bounds__(256, MINB)
     }
     const float4 *prow = plane + (long long)m2 * N;
     const float4 *flrow = fdf + ((long long)a1 * N + a2) * N;
-    const long long lrow0 = (long long)line * N;
+    const long long lrow0 = ((long long)i1 * N + i2) * N;
     u64 rh[RUN], rl[RUN];  // f_m hi, lo (re, im lanes)
 #pragma unroll
     for (int a = 0; a < RUN; ++a) {
@@ -298,7 +346,15 @@ __global__ void __launch_bounds__(256, MINB)
           }
           __syncwarp();
           if (lane == 0 && q + DEPTH < nrows) {  // refill this slot with row q + DEPTH
-            const long long lflat = (long long)c0 * N + q + DEPTH;
+            const long long lflat = rf_base + rf_i3;
+            if (++rf_i3 == N) {
+              rf_i3 = 0;
+              if (++rf_i2 == N) {
+                rf_i2 = 0;
+                ++rf_pi;
+              }
+              rf_base = ((long long)plane_i1(rf_pi) * N + rf_i2) * N;
+            }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_expect_tx(&mybar[slot], seg_bytes);
             bulk_g2s(myring + (size_t)slot * 32 * RUN, B2 + lflat * p.KC + wcol, seg_bytes,
@@ -343,14 +399,6 @@ __global__ void __launch_bounds__(256, MINB)
         }
       }
     }
-    // next line
-    if (++i2 == N) {
-      i2 = 0;
-      ++i1;
-      a1 = (a1 + 1 == N) ? 0 : a1 + 1;
-    }
-    a2 = (a2 + 1 == N) ? 0 : a2 + 1;
-    m2 = (m2 == 0) ? N - 1 : m2 - 1;
   }
   if (TMA) {
     if (__syncthreads_or(to)) {
@@ -397,23 +445,32 @@ static size_t c64x_smem(int N, int threads, bool tma) {
 // Tile shape, TMA eligibility and the line-chunk count that makes the grid
 // whole waves of resident CTAs (cached per shape: the occupancy query is not
 // free).
-static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int minb);
-static C64xPlan c64x_plan(const QParams &p, bool aligned, int minb) {
+// l-lines of the longest plane list (all N^2 lines, or about half when paired)
+static int c64x_lines(const QParams &p, bool paired) {
+  if (!paired) return p.N * p.N;
+  int m = 0;
+  for (int k1 = 0; k1 < p.N; ++k1) m = std::max(m, k1 / 2 + 1 + std::max(0, (k1 + p.N) / 2 - k1));
+  return m * p.N;
+}
+
+static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int minb, bool paired);
+static C64xPlan c64x_plan(const QParams &p, bool aligned, int minb, bool paired) {
   static std::mutex mu;
   static std::map<long long, C64xPlan> cache;
   int dev = 0;
   cudaGetDevice(&dev);
   const long long key =
-      ((((long long)dev * 128 + p.N) * 4 + p.mode) * 2 + (aligned ? 1 : 0)) * 4 + minb;
+      (((((long long)dev * 128 + p.N) * 4 + p.mode) * 2 + (aligned ? 1 : 0)) * 4 + minb) * 2 +
+      (paired ? 1 : 0);
   std::lock_guard<std::mutex> lock(mu);
   auto it = cache.find(key);
   if (it != cache.end()) return it->second;
-  C64xPlan pl = c64x_plan_compute(p, aligned, minb);
+  C64xPlan pl = c64x_plan_compute(p, aligned, minb, paired);
   cache[key] = pl;
   return pl;
 }
 
-static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int minb) {
+static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int minb, bool paired) {
   C64xPlan pl;
   const int R4 = (p.P + RUN - 1) / RUN;
   int J2T = 256 / R4;
@@ -435,7 +492,7 @@ static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int minb) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long long wave = (long long)sms * occ;
   const long long per_chunk = (long long)p.P * tiles;
-  const int NL = p.N * p.N;
+  const int NL = c64x_lines(p, paired);
   // chunk count that best fills whole waves (at most 8) with balanced chunks:
   // efficiency = useful CTA-lines / (waves * wave * lines per chunk)
   double best_eff = -1.0;
@@ -462,11 +519,12 @@ int calq64x_nchunk(const QParams &p, int *J2T_out) {
   // upper bound over the variants, used to size the partial-sum buffer
   int n = 1;
   for (int minb = 1; minb <= 2; ++minb)
-    for (int al = 0; al <= 1; ++al) {
-      const C64xPlan pl = c64x_plan(p, al != 0, minb);
-      if (J2T_out) *J2T_out = pl.J2T;
-      if (pl.nch > n) n = pl.nch;
-    }
+    for (int al = 0; al <= 1; ++al)
+      for (int pa = 0; pa <= 1; ++pa) {
+        const C64xPlan pl = c64x_plan(p, al != 0, minb, pa != 0);
+        if (J2T_out) *J2T_out = pl.J2T;
+        if (pl.nch > n) n = pl.nch;
+      }
   return n;
 }
 
@@ -482,25 +540,34 @@ edb_status launch_split_B(long long n, const double *B, float2 *B2, cudaStream_t
   return EDB_OK;
 }
 
+edb_status launch_split_B_paired(int N, const double *B, float2 *B2, cudaStream_t st) {
+  const long long n = (long long)N * N * N * N * N * N;
+  b2_pair_split_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(N, B, B2);
+  EDB_LAUNCHED();
+  return EDB_OK;
+}
+
 edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const float4 *d_fdf,
-                          double2 *d_partial, double2 *d_Q, cudaStream_t st, int minb) {
+                          double2 *d_partial, double2 *d_Q, cudaStream_t st, int minb,
+                          bool paired) {
   if (minb != 1) minb = 2;
+  if (paired && p.mode != EDB_INDEX_ALIASED) return fail(EDB_EINVAL, "calq64x: pairs need ALIASED");
   const bool aligned = ((uintptr_t)d_B2 % 16) == 0;
-  const C64xPlan pl = c64x_plan(p, aligned, minb);
+  const C64xPlan pl = c64x_plan(p, aligned, minb, paired);
   dim3 grid((unsigned)p.P, (unsigned)pl.tiles, (unsigned)pl.nch);
   if (pl.tma) {
     if (minb == 2)
-      calq64x_kernel<true, 2><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, d_B2, d_fdf,
+      calq64x_kernel<true, 2><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf,
                                                                  d_partial);
     else
-      calq64x_kernel<true, 1><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, d_B2, d_fdf,
+      calq64x_kernel<true, 1><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf,
                                                                  d_partial);
   } else {
     if (minb == 2)
-      calq64x_kernel<false, 2><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, d_B2, d_fdf,
+      calq64x_kernel<false, 2><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf,
                                                                   d_partial);
     else
-      calq64x_kernel<false, 1><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, d_B2, d_fdf,
+      calq64x_kernel<false, 1><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf,
                                                                   d_partial);
   }
   EDB_LAUNCHED();
