@@ -188,9 +188,13 @@ static int amax_of(int N) {
   return 3 * hi * hi;
 }
 
-// The double-float kernel's table: in ALIASED mode the symmetric pair table
-// (half the l1 planes are visited), else B split as it is.
-static bool qcalc_b2_paired(const edb_qcalc *q) { return q->p.mode == EDB_INDEX_ALIASED; }
+// The double-float kernel's table: the symmetric pair table (half the l1
+// planes are visited) in ALIASED mode and for odd N, where the REFERENCE index
+// mode is the same aliased convolution (P = N, the same index shifts); else
+// B split as it is.
+static bool qcalc_b2_paired(const edb_qcalc *q) {
+  return q->p.mode == EDB_INDEX_ALIASED || (q->p.N % 2 == 1 && q->p.P == q->p.N);
+}
 static edb_status qcalc_split_B2(edb_qcalc *q) {
   if (qcalc_b2_paired(q)) return launch_split_B_paired(q->p.N, q->B64, q->B2, q->st);
   return launch_split_B(q->p.NQ * q->p.NQ, q->B64, q->B2, q->st);

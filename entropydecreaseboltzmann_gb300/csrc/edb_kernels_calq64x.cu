@@ -551,7 +551,8 @@ edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const float4 *d_
                           double2 *d_partial, double2 *d_Q, cudaStream_t st, int minb,
                           bool paired) {
   if (minb != 1) minb = 2;
-  if (paired && p.mode != EDB_INDEX_ALIASED) return fail(EDB_EINVAL, "calq64x: pairs need ALIASED");
+  if (paired && (p.P != p.N || (p.sM % p.N) != 0 || (p.sL % p.N) != p.N - p.n))
+    return fail(EDB_EINVAL, "calq64x: pairs need the aliased index shifts");
   const bool aligned = ((uintptr_t)d_B2 % 16) == 0;
   const C64xPlan pl = c64x_plan(p, aligned, minb, paired);
   dim3 grid((unsigned)p.P, (unsigned)pl.tiles, (unsigned)pl.nch);
