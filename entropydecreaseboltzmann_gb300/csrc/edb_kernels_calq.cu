@@ -1085,7 +1085,7 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
                    ((uintptr_t)src % 16) == 0;
   // line staging by two tensor copies when the f_l box fits (<= 256 floats a
   // row), else by one bulk copy per B row and f_l line
-  C32Maps maps;
+  C32Maps maps{};
   if (tma && 2 * c32_geom(N, A, K2T, 1, 1, 0, units, el, true).FLS <= 256 && N <= 256) {
     const int FLS = c32_geom(N, A, K2T, 1, 1, 0, units, el, true).FLS;
     const long long NQ = (long long)N * N * N;

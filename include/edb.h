@@ -108,8 +108,12 @@ edb_status edb_qcalc_destroy(edb_qcalc *q);
 edb_status edb_qcalc_close_filter(edb_qcalc *q);
 
 /* genB (QCalculator.h:158-229) on the device in FP64: the N^3 x N^3 table
- * beta(l, k), plus (ALIASED mode) its FP32 copy in FFTW order for the batched
- * path.  gamma outside {0,1} uses Gauss-Legendre quadrature of
+ * beta(l, k) (what edb_qcalc_copy_B returns), plus the kernels' own forms:
+ * in ALIASED mode (and for odd N) the symmetric pair table
+ * beta(l, k) + beta(k - l, k) that lets each Q-hat kernel visit half the
+ * l1 planes, as FP32 in FFTW order for the batched path and split into
+ * (hi, lo) floats for the double-float FP64 kernel.  gamma outside {0,1}
+ * uses Gauss-Legendre quadrature of
  * F_gamma = int_0^1 r^(2+gamma) sinc(xi r) sinc(eta r) dr (ReadMe.md:51). */
 edb_status edb_qcalc_genB(edb_qcalc *q);
 
@@ -122,7 +126,7 @@ edb_status edb_funF(int alpha, long long n, const double *xi, const double *eta,
 edb_status edb_filtering(int N, long long n, const int *beta, double *out);
 
 /* genB for batched use only (ALIASED mode): builds just the FP32 FFTW-order
- * table (4 bytes per entry instead of 8 + 8 + 4), so many tables fit in one
+ * pair table (4 bytes per entry instead of 8 + 8 + 4), so many tables fit in one
  * HBM budget.  The FP64 calQ entry points then report EDB_ENOTREADY. */
 edb_status edb_qcalc_genB_f32(edb_qcalc *q);
 
@@ -204,7 +208,7 @@ typedef struct {
   long long NQ;         /* N^3 */
   long long terms;      /* terms of one calQ: N^3 P^3 */
   long long B_bytes;    /* FP64 table bytes */
-  int has_B32;          /* FP32 FFTW-order copy present */
+  int has_B32;          /* FP32 FFTW-order pair table present */
 } edb_qcalc_info;
 edb_status edb_qcalc_get_info(edb_qcalc *q, edb_qcalc_info *out);
 
