@@ -83,7 +83,9 @@ def test_calQ_fp64_aliased_bkw(edb, oracle, N, L):
     assert rel_l2(q.calQ(None, fhat), Qo) <= 1e-12
 
 
-@pytest.mark.parametrize("N", [5, 6, 8, 16])
+# radix-4/2 stages, odd-prime stages (3, 5, 7), primes taken whole (17), and
+# N = 64 (the 131 KB shared-memory tile of the FP64 pass)
+@pytest.mark.parametrize("N", [2, 3, 5, 6, 8, 12, 16, 17, 21, 24, 25, 32, 64])
 def test_fft3d_matches_oracle(edb, oracle, N):
     rng = np.random.default_rng(N)
     x = rng.standard_normal(N ** 3) + 1j * rng.standard_normal(N ** 3)
