@@ -156,10 +156,13 @@ edb_status launch_calq64_reduce(const QParams &p, int nchunk, const double2 *d_p
 // Batched FP32 kernel (ALIASED mode, many solves sharing one table).
 //
 // Work: Q^s_K = sum_L B[L][K] f^s_L f^s_((K-L) mod N) for S solves; every index
-// in FFTW order, B32 row-major [L][K].
+// in FFTW order.  The terms L and M = K - L carry the same product, so B32
+// (row-major [L][K]) is the symmetric pair table B[L][K] + B[M][K] written by
+// genB_kernel, and only the l1 planes with l1 <= (k1 - l1) mod N are summed:
+// [0, k1/2] and [k1+1, (k1+N)/2], about half of them.
 //
 // CTA = (group of SG = 2 WS solves) x (one k1, a tile of K2T k2 values, all
-// k3) x (a chunk of l1 planes).  Thread = (solve pair {w, w+WS}, k2, run of
+// k3) x (a chunk of those l1 planes).  Thread = (solve pair {w, w+WS}, k2, run of
 // A = 8 or 4 consecutive k3).  WS = 8 (16-solve groups) for throughput; WS = 2
 // (4-solve groups) for the few live solves of a serving table.  The CTA walks
 // the l-lines (l1, l2) of its chunk in order; for each line it needs
@@ -188,11 +191,12 @@ edb_status launch_calq64_reduce(const QParams &p, int nchunk, const double2 *d_p
 // terms per output), then combined and folded into a (hi, lo) two-sum pair:
 // blocked compensated summation.
 //
-// Chunks: with C > 1 the l1 planes are split into C consecutive chunks so that
-// a few solves still fill the GPU; each chunk writes its (hi, lo) pairs and
-// calq32_reduce_kernel adds the chunks in order in FP64.  The chunk
-// boundaries depend only on (N, C), never on S or the variant, so a solve's
-// result does not depend on what else is in the batch.
+// Chunks: with C > 1 the visited l1 planes are split into C consecutive chunks
+// so that a few solves still fill the GPU; each chunk writes its (hi, lo) pairs
+// and calq32_reduce_kernel adds the chunks in order in FP64 (a chunk may be
+// empty: it writes zeros).  The chunk boundaries depend only on (N, C, k1),
+// never on S or the variant, so a solve's result does not depend on what else
+// is in the batch.
 // ---------------------------------------------------------------------------
 namespace {
 constexpr int SC = 2;                     // solves per thread: w and w + WS

@@ -24,8 +24,13 @@
 // with every operation a packed f32x2 instruction over (re, im) lanes; at the
 // end Q = (A.re - B.im, A.im + B.re), combined in FP64.
 //
-// Tiling: CTA = (output plane j1, a tile of j2, all j3) x (a chunk of l-lines
-// (i1, i2)).  Thread = (j2, run of 4 consecutive j3).  For each i1 the f-hat
+// Pairs: with the aliased index shifts (ALIASED mode, or odd N) B2 is the
+// split symmetric pair table (b2_pair_split_kernel) and each output plane
+// visits only the l1 planes with l1 <= (k1 - l1) mod N, about half the B
+// stream; otherwise every l-line is visited with B split as it is.
+//
+// Tiling: CTA = (output plane j1, a tile of j2, all j3) x (a chunk of its
+// l-lines (i1, i2)).  Thread = (j2, run of 4 consecutive j3).  For each i1 the f-hat
 // m1-plane (m1 = j1 - i1 + sM mod N) is staged in shared memory; along i3 the
 // needed f_m slide down by one (a ring of 4).  The number of line chunks is
 // set from the measured occupancy so the grid is whole waves.  Each CTA writes
