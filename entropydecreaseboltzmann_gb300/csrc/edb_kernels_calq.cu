@@ -686,6 +686,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
   const int nwarps = (blockDim.x + 31) >> 5;
+  const int nfull = max(1, (int)blockDim.x / 32);  // warps with 32 lanes
   const int w = tid % WS;
   const int rest = tid / WS;
   const int r = rest % g.R;
@@ -766,9 +767,10 @@ __global__ void __launch_bounds__(MAXT, MINB)
 
   // Pipeline bookkeeping uses chunk-relative indices: j (line), pr (plane).
   // prologue: lines 0 .. NST-2 and the first plane
-  int issued = 0, planes = 0;  // counted in warp 0
+  int planes = 0;       // counted in warp 0
+  int jstop = nlines;   // first line not finished by every warp (abort drain)
   if (TMA && warp == 0 && nlines > 0) {
-    for (int j = 0; j < NST - 1 && j < nlines; ++j, ++issued)
+    for (int j = 0; j < NST - 1 && j < nlines; ++j)
       stage_line<true>(g, line_li(j), j % NST, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls,
                        full, tmap, &tmB, &tmF);
     stage_plane<true>(g, (k1 - plane_l1(P0) + N) % N, u0, nval, NQ, fin, plb, &pbar[0]);
@@ -786,6 +788,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
       // every warp is done with the previous plane (and with its buffer)
       if (__syncthreads_or(to)) {
         aborted = true;
+        jstop = j;
         break;
       }
       if (TMA) {
@@ -808,14 +811,16 @@ __global__ void __launch_bounds__(MAXT, MINB)
       }
     }
     if (TMA) {
-      // refill: line j+NST-1 goes into the stage line j-1 used
+      // refill: line j+NST-1 goes into the stage line j-1 used.  The issuing
+      // warp rotates over the full warps with the line, so the issue work
+      // (and the wait for every warp to leave line j-1) does not make one warp
+      // fall behind the rest.
       const int jn = j + NST - 1;
-      if (warp == 0 && jn < nlines) {
+      if (warp == jn % nfull && jn < nlines) {
         const int sn = jn % NST;
         if (j >= 1) mbar_wait(&empty[sn], (uint32_t)(((j - 1) / NST) & 1), to);
         stage_line<true>(g, line_li(jn), sn, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full,
                          tmap, &tmB, &tmF);
-        ++issued;
       }
       mbar_wait(&full[st], (uint32_t)((j / NST) & 1), to);
     } else {
@@ -883,6 +888,9 @@ __global__ void __launch_bounds__(MAXT, MINB)
       // lands after the block exits
       bool t2 = false;
       if (TMA) {
+        // every warp finished iterations 0 .. jstop-1, each of which issued
+        // line i + NST - 1 after the NST - 1 lines of the prologue
+        const int issued = min(nlines, jstop + NST - 1);
         for (int sx = 0; sx < NST; ++sx) {
           int last = -1;  // last line issued into stage sx
           for (int x = issued - 1; x >= 0 && x >= issued - NST; --x)
