@@ -6,10 +6,10 @@
 // tile of a cube (N lines of the transform axis) into shared memory, line by
 // line, and runs a mixed-radix Stockham FFT on every line: N = r_1 r_2 ... r_m
 // with radix-4 and radix-2 stages first (butterflies of additions and +-i
-// swaps), then the odd prime factors in ascending order.  An odd-radix stage
-// computes each of its outputs as one sum of R terms against the twiddle table
-// exp(sign 2 pi i m/N) (the stage's input twiddle and its R-point DFT folded
-// into one table index), so a prime N is the direct DFT.  Stockham's
+// swaps), then the odd prime factors in ascending order: radix 3 as a
+// butterfly, any other odd radix R as one sum of R terms per output against
+// the twiddle table exp(sign 2 pi i m/N) (the stage's input twiddle and its
+// R-point DFT folded into one table index), so a prime N is the direct DFT.  Stockham's
 // self-sorting form ping-pongs between two line buffers and leaves the result
 // in natural order.  The per-point cost is sum(r_i) complex operations instead
 // of N, e.g. 4 + 2 + 3 against 24 at N = 24.
@@ -69,9 +69,9 @@ __device__ __forceinline__ R2 c_mul(R2 a, R2 w) {
   return r;
 }
 
-// One Stockham stage of radix R (2 or 4) on every line of the tile: butterfly
-// j of a line reads src[j + i M] (M = N / R), applies the input twiddles
-// w^(i tstep), does the R-point DFT and writes dst[expand(j) + q Ns].
+// One Stockham stage of radix R (2, 3 or 4) on every line of the tile:
+// butterfly j of a line reads src[j + i M] (M = N / R), applies the input
+// twiddles w^(i tstep), does the R-point DFT and writes dst[expand(j) + q Ns].
 template <int R, typename R2>
 __device__ __forceinline__ void fft_stage_pow2(int N, int LS, int Ns, int sign, const R2 *src,
                                                R2 *dst, const R2 *tw) {
@@ -90,6 +90,19 @@ __device__ __forceinline__ void fft_stage_pow2(int N, int LS, int Ns, int sign, 
     if (R == 2) {
       dl[d0] = c_add(v[0], v[1]);
       dl[d0 + Ns] = c_sub(v[0], v[1]);
+    } else if (R == 3) {
+      // w3 = exp(sign 2 pi i / 3) = (-1/2, h), h = tw[N / 3].y = sign sqrt(3)/2:
+      // o0 = v0 + s, o1,2 = v0 - s/2 +- i h d  (s = v1 + v2, d = v1 - v2)
+      const R2 sm = c_add(v[1], v[2]), df = c_sub(v[1], v[2]);
+      const auto h = tw[N / 3].y;
+      R2 t, u;
+      t.x = v[0].x - 0.5f * sm.x;
+      t.y = v[0].y - 0.5f * sm.y;
+      u.x = -h * df.y;
+      u.y = h * df.x;
+      dl[d0] = c_add(v[0], sm);
+      dl[d0 + Ns] = c_add(t, u);
+      dl[d0 + 2 * Ns] = c_sub(t, u);
     } else {
       // w4 = exp(sign 2 pi i / 4) = sign i; (v1 - v3) w4
       const R2 a = c_add(v[0], v[2]), b = c_sub(v[0], v[2]), c = c_add(v[1], v[3]);
@@ -189,6 +202,8 @@ __global__ void fft_pass_kernel(int N, int axis, int sign, R scale, FftPlan plan
       fft_stage_pow2<4>(N, LS, Ns, sign, src, dst, tw);
     else if (Rd == 2)
       fft_stage_pow2<2>(N, LS, Ns, sign, src, dst, tw);
+    else if (Rd == 3)
+      fft_stage_pow2<3>(N, LS, Ns, sign, src, dst, tw);
     else
       fft_stage_direct<R2, R>(N, LS, Rd, Ns, src, dst, tw);
     __syncthreads();
