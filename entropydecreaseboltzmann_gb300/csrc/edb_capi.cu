@@ -80,7 +80,7 @@ struct edb_qcalc {
   cudaStream_t st = nullptr;
   double *B64 = nullptr;    // [l][k] centred, N^3 x N^3 (flat stream of row stride KC)
   float2 *B2 = nullptr;     // B64 split into (hi, lo) floats, same layout
-  float *B32 = nullptr;     // FFTW order [l][k] (ALIASED only)
+  float *B32 = nullptr;     // FP32 pair table, FFTW order [l1 l2][k1][l3][k2][k3] (ALIASED)
   float4 *fdf = nullptr;    // input split for the double-float kernel
   int fp64_kernel = EDB_FP64_EMULATED;
   int c64x_minb = 2;    // register cap of the double-float kernel, tuned at genB

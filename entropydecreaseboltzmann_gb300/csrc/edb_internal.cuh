@@ -80,7 +80,8 @@ edb_status launch_ftable(int N, double gamma, double *d_T, int amax, cudaStream_
 // sigma (filter) per centred index and Bmm per flat centred index.
 edb_status launch_bmm(int N, double gamma, double L, int filter, int mode, const double *d_T,
                       int amax, double *d_sigma, double *d_Bmm, cudaStream_t st);
-// B64: [l][k] centred, N^3 x N^3 doubles.  B32 (optional): FFTW order floats.
+// B64: [l][k] centred, N^3 x N^3 doubles.  B32 (optional): the FP32 pair table
+// in FFTW order, [l1 l2][k1][l3][k2][k3] (see genB_kernel).
 edb_status launch_genB(int N, double gamma, double L, int filter, int mode, const double *d_T,
                        int amax, const double *d_sigma, const double *d_Bmm, double *d_B64,
                        float *d_B32, cudaStream_t st);

@@ -156,10 +156,10 @@ edb_status launch_calq64_reduce(const QParams &p, int nchunk, const double2 *d_p
 // Batched FP32 kernel (ALIASED mode, many solves sharing one table).
 //
 // Work: Q^s_K = sum_L B[L][K] f^s_L f^s_((K-L) mod N) for S solves; every index
-// in FFTW order.  The terms L and M = K - L carry the same product, so B32
-// (row-major [L][K]) is the symmetric pair table B[L][K] + B[M][K] written by
-// genB_kernel, and only the l1 planes with l1 <= (k1 - l1) mod N are summed:
-// [0, k1/2] and [k1+1, (k1+N)/2], about half of them.
+// in FFTW order.  The terms L and M = K - L carry the same product, so B32 is
+// the symmetric pair table B[L][K] + B[M][K] written by genB_kernel (laid out
+// [l1 l2][k1][l3][k2][k3]), and only the l1 planes with l1 <= (k1 - l1) mod N
+// are summed: [0, k1/2] and [k1+1, (k1+N)/2], about half of them.
 //
 // CTA = (group of SG = 2 WS solves) x (one k1, a tile of K2T k2 values, all
 // k3) x (a chunk of those l1 planes).  Thread = (solve pair {w, w+WS}, k2, run of
@@ -403,8 +403,9 @@ __device__ __forceinline__ void two_sum_fold2(u64 &hi, u64 &lo, u64 x) {
 
 
 // Tensor copies (one elected thread): the B tile of line li is one 5-D box
-// {k3: N, k2: K2T, k1: 1, l3: N, line: 1} of the table viewed as
-// [line][l3][k1][k2][k3]; the f_l lines of the group are one 3-D box
+// {k3: N, k2: K2T, l3: N, k1: 1, line: 1} of the table, stored as
+// [line][k1][l3][k2][k3] so the tile's rows lie within N^3 floats; the f_l
+// lines of the group are one 3-D box
 // {FLS floats x 2, 1 line, SG units} of the input viewed as [unit][line][l3],
 // whose columns past N*EL complex are out of bounds and land as zeros.
 __device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *tm, int c0, int c1,
@@ -438,7 +439,9 @@ __device__ __forceinline__ void stage_line(const C32Geom &g, int li, int st, int
   const int N = g.N;
   float *Bd = Bs + (size_t)st * g.BSTG;
   float2 *fd = fls + (size_t)st * g.FSTG;
-  const float *Bsrc = B32 + (long long)li * N * NQ + (long long)k1 * N * N + (long long)k2_0 * N;
+  // table layout [line][k1][l3][k2][k3]: the tile's rows l3 are N^2 apart
+  const float *Bsrc = B32 + ((long long)li * N + k1) * NQ + (long long)k2_0 * N;
+  const long long NN = (long long)N * N;
   const int EL = g.EL;  // s0 / nval count data units of EL float2 per element
   const float2 *fsrc = fin + ((long long)s0 * NQ + (long long)li * N) * EL;
   const int rowlen = k2n * N;
@@ -446,7 +449,7 @@ __device__ __forceinline__ void stage_line(const C32Geom &g, int li, int st, int
     if ((threadIdx.x & 31) == 0) {
       mbar_expect_tx(full + st, (uint32_t)(N * g.K2T * N * 4 + g.SG * g.FLS * 8));
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      tma_load_5d(Bd, tmB, 0, k2_0, k1, 0, li, full + st);
+      tma_load_5d(Bd, tmB, 0, k2_0, 0, k1, li, full + st);
       tma_load_3d(fd, tmF, 0, li, s0, full + st);
     }
     __syncwarp(warp_mask());
@@ -456,13 +459,13 @@ __device__ __forceinline__ void stage_line(const C32Geom &g, int li, int st, int
     __syncwarp(warp_mask());
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     for (int l3 = lane; l3 < N; l3 += 32)
-      bulk_g2s(Bd + (size_t)l3 * g.BROW, Bsrc + (long long)l3 * NQ, rowlen * 4, full + st);
+      bulk_g2s(Bd + (size_t)l3 * g.BROW, Bsrc + (long long)l3 * NN, rowlen * 4, full + st);
     for (int s = lane; s < nval; s += 32)
       bulk_g2s(fd + (size_t)s * g.FLS, fsrc + (long long)s * NQ * EL, N * 8 * EL, full + st);
   } else {
     for (int e = threadIdx.x; e < N * rowlen; e += blockDim.x) {
       int l3 = e / rowlen, c = e % rowlen;
-      Bd[(size_t)l3 * g.BROW + c] = __ldg(Bsrc + (long long)l3 * NQ + c);
+      Bd[(size_t)l3 * g.BROW + c] = __ldg(Bsrc + (long long)l3 * NN + c);
     }
     for (int e = threadIdx.x; e < nval * N * EL; e += blockDim.x) {
       int s = e / (N * EL), j = e % (N * EL);
@@ -1105,7 +1108,8 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
                                 (cuuint64_t)N * N};
     const cuuint64_t bstr[4] = {(cuuint64_t)N * 4, (cuuint64_t)N * N * 4, (cuuint64_t)NQ * 4,
                                 (cuuint64_t)N * NQ * 4};
-    const cuuint32_t bbox[5] = {(cuuint32_t)N, (cuuint32_t)K2T, 1, (cuuint32_t)N, 1};
+    // table [line][k1][l3][k2][k3]: dims k3, k2, l3, k1, line
+    const cuuint32_t bbox[5] = {(cuuint32_t)N, (cuuint32_t)K2T, (cuuint32_t)N, 1, 1};
     const long long nunits = vr.pair ? (S + 1) / 2 : S;
     const cuuint64_t fdim[3] = {(cuuint64_t)N * 2 * el, (cuuint64_t)N * N, (cuuint64_t)nunits};
     const cuuint64_t fstr[2] = {(cuuint64_t)N * 8 * el, (cuuint64_t)NQ * 8 * el};
