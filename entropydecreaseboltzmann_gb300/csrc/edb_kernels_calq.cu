@@ -169,9 +169,10 @@ edb_status launch_calq64_reduce(const QParams &p, int nchunk, const double2 *d_p
 //   B[(l1,l2,l3)][k1, k2-tile, all k3]  N rows of K2T*N floats (the B tile),
 //   f^s[l1][l2][:]                       N complex per solve (the f_l line),
 //   f^s[m1][:][:], m1 = k1 - l1          the m1-plane, kept while l1 is fixed.
-// Tile and line are double-buffered in shared memory.  Warp 0 issues the 1-D
-// TMA bulk copies (cp.async.bulk ... mbarrier::complete_tx) of line i+1, one
-// copy per lane, while every warp computes line i; a "full" mbarrier per
+// Tile and line live in NST = 2-4 shared-memory stages.  One warp (rotating
+// with the line) issues the TMA copies of line i + NST - 1 (two tensor copies,
+// cp.async.bulk.tensor ... mbarrier::complete_tx; or 1-D bulk copies, one per
+// row and per solve) while every warp computes line i; a "full" mbarrier per
 // stage says the data landed, an "empty" mbarrier per stage (one arrival per
 // warp) says every warp is done with it, so warps never wait for each other
 // inside an l1-plane.  All waits are bounded: a wait that runs out marks the
@@ -426,8 +427,8 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, in
       : "memory");
 }
 
-// Issue (TMA: warp 0; tensor copies from one thread, or one bulk copy per B
-// row and f_l line from each lane) or perform (plain: all threads) the
+// Issue (TMA: one whole warp; tensor copies from its lane 0, or one bulk copy
+// per B row and f_l line from each lane) or perform (plain: all threads) the
 // staging of the B tile and f_l line of line li into buffer `st`.
 template <bool TMA>
 __device__ __forceinline__ void stage_line(const C32Geom &g, int li, int st, int k1, int k2_0,
@@ -445,7 +446,7 @@ __device__ __forceinline__ void stage_line(const C32Geom &g, int li, int st, int
   const int EL = g.EL;  // s0 / nval count data units of EL float2 per element
   const float2 *fsrc = fin + ((long long)s0 * NQ + (long long)li * N) * EL;
   const int rowlen = k2n * N;
-  if (TMA && tmap) {  // called by warp 0 only
+  if (TMA && tmap) {  // called by the issuing warp only
     if ((threadIdx.x & 31) == 0) {
       mbar_expect_tx(full + st, (uint32_t)(N * g.K2T * N * 4 + g.SG * g.FLS * 8));
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -453,7 +454,7 @@ __device__ __forceinline__ void stage_line(const C32Geom &g, int li, int st, int
       tma_load_3d(fd, tmF, 0, li, s0, full + st);
     }
     __syncwarp(warp_mask());
-  } else if (TMA) {  // called by warp 0 only
+  } else if (TMA) {  // called by the issuing warp only (a full warp)
     const int lane = threadIdx.x & 31;
     if (lane == 0) mbar_expect_tx(full + st, (uint32_t)(N * rowlen * 4 + nval * N * 8 * EL));
     __syncwarp(warp_mask());
