@@ -1041,7 +1041,13 @@ struct edb_batch {
   cudaGraphExec_t exec = nullptr;
   cudaStream_t exec_stream = nullptr;
   int launches_per_step = 0;
+  // host transfers of load/read in cube chunks on their own stream, so the
+  // copy of one chunk overlaps the transforms of the next
+  cudaStream_t cst = nullptr;
+  cudaEvent_t xev[8] = {};
 };
+
+static constexpr int BATCH_XFER_CHUNKS = 8;
 
 extern "C" edb_status edb_batch_create(edb_qcalc *q, const edb_batch_desc *d, edb_batch **out) {
   if (!q || !d || !out) return fail(EDB_EINVAL, "null argument");
@@ -1061,6 +1067,11 @@ extern "C" edb_status edb_batch_create(edb_qcalc *q, const edb_batch_desc *d, ed
   edb_status rc = EDB_OK;
   cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
   if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamCreate");
+  if (rc == EDB_OK && (e = cudaStreamCreateWithFlags(&b->cst, cudaStreamNonBlocking)) != cudaSuccess)
+    rc = cuda_fail(e, "cudaStreamCreate");
+  for (int i = 0; i < BATCH_XFER_CHUNKS && rc == EDB_OK; ++i)
+    if ((e = cudaEventCreateWithFlags(&b->xev[i], cudaEventDisableTiming)) != cudaSuccess)
+      rc = cuda_fail(e, "cudaEventCreate");
   if (rc == EDB_OK) rc = dalloc(&b->Fhat, n);
   if (rc == EDB_OK) rc = dalloc(&b->F, n);
   const int nstage = d->scheme == EDB_SCHEME_RK4 ? 3 : (d->scheme == EDB_SCHEME_SSP3 ? 2 : 0);
@@ -1105,14 +1116,19 @@ extern "C" edb_status edb_batch_destroy(edb_batch *b) {
   dfree(b->tr_fixed);
   dfree(b->ctab);
   dfree(b->m0);
+  for (auto &ev : b->xev)
+    if (ev) cudaEventDestroy(ev);
+  if (b->cst) cudaStreamDestroy(b->cst);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
   return EDB_OK;
 }
 
-static edb_status batch_init_state(edb_batch *b, cudaStream_t st) {
+// transformed: Fhat already holds fft(F) (the chunked host load does it per
+// chunk as the chunks arrive).
+static edb_status batch_init_state(edb_batch *b, cudaStream_t st, bool transformed = false) {
   // Fhat = fft(F) in FP64, its FP32 copy, entropy bookkeeping reset
-  EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->F, b->Fhat, nullptr, 0, 0, st));
+  if (!transformed) EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->F, b->Fhat, nullptr, 0, 0, st));
   if (b->d.conserve) EDB_TRY(launch_hat_moments(b->d.N, b->d.S, b->ctab, b->Fhat, b->m0, st));
   EDB_TRY(launch_d2f(b->n, b->Fhat, b->in32, st));
   // pick the batched kernel's variant for this S on real data, before the
@@ -1134,12 +1150,33 @@ static edb_status batch_init_state(edb_batch *b, cudaStream_t st) {
 // S x N^3 doubles of bytes) is free; load and read stage real-space data in it.
 static double *batch_staging(edb_batch *b) { return reinterpret_cast<double *>(b->Qs[0]); }
 
+// Cube range [c0, c1) of transfer chunk i.
+static void batch_chunk(const edb_batch *b, int i, int *c0, int *c1) {
+  const int per = (b->d.S + BATCH_XFER_CHUNKS - 1) / BATCH_XFER_CHUNKS;
+  *c0 = std::min(b->d.S, i * per);
+  *c1 = std::min(b->d.S, *c0 + per);
+}
+
 extern "C" edb_status edb_batch_load(edb_batch *b, const double *F0_real) {
   if (!b || !F0_real) return fail(EDB_EINVAL, "null argument");
   double *stage = batch_staging(b);
-  EDB_CUDA(cudaMemcpyAsync(stage, F0_real, sizeof(double) * b->n, cudaMemcpyHostToDevice, b->st));
-  EDB_TRY(launch_real_to_complex(b->n, stage, b->F, b->st));
-  return batch_init_state(b, b->st);
+  const long long NQ = b->NQ;
+  // the staging buffer is free once the previous work on st is done
+  EDB_CUDA(cudaEventRecord(b->xev[0], b->st));
+  EDB_CUDA(cudaStreamWaitEvent(b->cst, b->xev[0], 0));
+  for (int i = 0; i < BATCH_XFER_CHUNKS; ++i) {  // copy chunk i while chunk i-1 transforms
+    int c0, c1;
+    batch_chunk(b, i, &c0, &c1);
+    if (c1 <= c0) break;
+    EDB_CUDA(cudaMemcpyAsync(stage + c0 * NQ, F0_real + c0 * NQ, sizeof(double) * (c1 - c0) * NQ,
+                             cudaMemcpyHostToDevice, b->cst));
+    EDB_CUDA(cudaEventRecord(b->xev[i], b->cst));
+    EDB_CUDA(cudaStreamWaitEvent(b->st, b->xev[i], 0));
+    EDB_TRY(launch_real_to_complex((c1 - c0) * NQ, stage + c0 * NQ, b->F + c0 * NQ, b->st));
+    EDB_TRY(launch_dft3d(b->d.N, c1 - c0, b->F + c0 * NQ, b->Fhat + c0 * NQ, nullptr, 0, 0,
+                         b->st));
+  }
+  return batch_init_state(b, b->st, true);
 }
 
 extern "C" edb_status edb_batch_load_device(edb_batch *b, const double *d_F0_real, void *stream) {
@@ -1247,11 +1284,22 @@ extern "C" edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat)
   EDB_CUDA(cudaStreamSynchronize(st));
   if (Fhat)
     EDB_CUDA(cudaMemcpyAsync(Fhat, b->Fhat, sizeof(double2) * b->n, cudaMemcpyDeviceToHost, st));
-  if (F_real) {  // inverse transform, real parts packed on the device
-    EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->Fhat, b->F, nullptr, 1, 0, st));
+  if (F_real) {  // inverse transform, real parts packed on the device, per
+                 // chunk: chunk i copies out while chunk i+1 transforms
     double *stage = batch_staging(b);
-    EDB_TRY(launch_complex_to_real(b->n, b->F, stage, st));
-    EDB_CUDA(cudaMemcpyAsync(F_real, stage, sizeof(double) * b->n, cudaMemcpyDeviceToHost, st));
+    const long long NQ = b->NQ;
+    for (int i = 0; i < BATCH_XFER_CHUNKS; ++i) {
+      int c0, c1;
+      batch_chunk(b, i, &c0, &c1);
+      if (c1 <= c0) break;
+      EDB_TRY(launch_dft3d(b->d.N, c1 - c0, b->Fhat + c0 * NQ, b->F + c0 * NQ, nullptr, 1, 0, st));
+      EDB_TRY(launch_complex_to_real((c1 - c0) * NQ, b->F + c0 * NQ, stage + c0 * NQ, st));
+      EDB_CUDA(cudaEventRecord(b->xev[i], st));
+      EDB_CUDA(cudaStreamWaitEvent(b->cst, b->xev[i], 0));
+      EDB_CUDA(cudaMemcpyAsync(F_real + c0 * NQ, stage + c0 * NQ, sizeof(double) * (c1 - c0) * NQ,
+                               cudaMemcpyDeviceToHost, b->cst));
+    }
+    EDB_CUDA(cudaStreamSynchronize(b->cst));
   }
   EDB_CUDA(cudaStreamSynchronize(st));
   return EDB_OK;
