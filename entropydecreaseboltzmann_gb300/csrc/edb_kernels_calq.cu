@@ -1037,13 +1037,12 @@ template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB, bool PAIR>
 static edb_status launch_c32(dim3 grid, int threads, size_t smem, int N, int S, int K2T, int NST,
                              int NPL, int C, int GB, const float *B32, const float2 *fin,
                              float2 *Q, float4 *partial, const C32Maps &maps, cudaStream_t st) {
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(calq32_kernel<TMA, MAXT, HLS, WS, A, MINB, PAIR>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(calq32)");
-    configured = true;
-  }
+  // once per instantiation (thread-safe static initialisation: the serving
+  // loop's thread and a caller's thread may launch concurrently)
+  static const cudaError_t configured =
+      cudaFuncSetAttribute(calq32_kernel<TMA, MAXT, HLS, WS, A, MINB, PAIR>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  if (configured != cudaSuccess) return cuda_fail(configured, "cudaFuncSetAttribute(calq32)");
   calq32_kernel<TMA, MAXT, HLS, WS, A, MINB, PAIR>
       <<<grid, threads, smem, st>>>(N, S, K2T, NST, NPL, C, GB, B32, fin, Q, partial, maps.tmap,
                                     maps.B, maps.F);

@@ -227,13 +227,10 @@ static edb_status dft3d_t(int N, int batch, const R2 *in, R2 *out, int inverse, 
   const int sign = inverse ? +1 : -1;
   const int threads = N * N < FFT_THREADS ? ((N * N + 31) / 32) * 32 : FFT_THREADS;
   const size_t smem = sizeof(R2) * (2 * (size_t)N * (N + 1) + N);
-  static bool configured = false;  // N = 64 in FP64 needs 131 KB
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(fft_pass_kernel<R2, R>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(fft_pass)");
-    configured = true;
-  }
+  // once per instantiation, thread-safe (N = 64 in FP64 needs 131 KB)
+  static const cudaError_t configured = cudaFuncSetAttribute(
+      fft_pass_kernel<R2, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  if (configured != cudaSuccess) return cuda_fail(configured, "cudaFuncSetAttribute(fft_pass)");
   const FftPlan plan = fft_plan(N);
   dim3 grid((unsigned)N, (unsigned)batch);
   const R one = (R)1;
