@@ -328,3 +328,26 @@ def test_funF_and_filtering_on_device_match_reference_golden(edb, golden):
         q = edb.QCalculator(N, 0)
         got = q.filtering(rows[:, 1].astype(np.int32))
         assert np.max(np.abs(got - rows[:, 2])) <= 1e-13 * np.max(np.abs(rows[:, 2]))
+
+
+@pytest.mark.parametrize("S", [1, 3, 11, 17])
+def test_batch_load_read_round_trip(edb, oracle, S):
+    """Load and read move the state in cube chunks on a second stream (S not a
+    multiple of the chunk count, fewer solves than chunks): read(load(f)) = f
+    to FFT round-off, into a caller's buffer too, and Fhat after load is the
+    FP64 transform of each solve (<= 1e-13 against the oracle's DFT)."""
+    N, L = 12, 6.0
+    rng = np.random.default_rng(300 + S)
+    f = rng.standard_normal((S, N ** 3))
+    q = edb.QCalculator(N, 0, L=L, filter=False, index_mode=INDEX_ALIASED)
+    q.genB()
+    b = edb.BatchSolver(q, S, L, edb.SCHEME_RK4, 0.01)
+    b.load(f)
+    back, fh = b.read(real=True, fhat=True)
+    assert np.max(np.abs(back - f)) <= 1e-13 * np.max(np.abs(f))
+    for s in range(S):
+        want = oracle.fft3d(N, f[s].astype(np.complex128))
+        assert np.max(np.abs(fh[s] - want)) <= 1e-13 * np.max(np.abs(want))
+    out = np.empty((S, N ** 3))
+    b.read(real=True, out=out)
+    assert np.array_equal(out, back)
