@@ -80,7 +80,7 @@ struct edb_qcalc {
   cudaStream_t st = nullptr;
   double *B64 = nullptr;    // [l][k] centred, N^3 x N^3 (flat stream of row stride KC)
   float2 *B2 = nullptr;     // B64 split into (hi, lo) floats, same layout
-  float *B32 = nullptr;     // FP32 pair table, FFTW order [l1 l2][k1][l3][k2][k3] (ALIASED)
+  float *B32 = nullptr;     // FP32 pair table, visited planes only (c32_table_floats; ALIASED)
   float4 *fdf = nullptr;    // input split for the double-float kernel
   int fp64_kernel = EDB_FP64_EMULATED;
   int c64x_minb = 2;    // register cap of the double-float kernel, tuned at genB
@@ -262,7 +262,7 @@ extern "C" edb_status edb_qcalc_genB(edb_qcalc *q) {
   if (!q->B64) EDB_TRY(dalloc(&q->B64, (size_t)NQ * NQ));
   if (!q->B2) EDB_TRY(dalloc(&q->B2, (size_t)NQ * NQ));
   if (q->d.index_mode == EDB_INDEX_ALIASED && !q->B32)
-    EDB_TRY(dalloc(&q->B32, (size_t)NQ * NQ + 64));  // +64: masked tail reads of calq32
+    EDB_TRY(dalloc(&q->B32, (size_t)c32_table_floats(N) + 64));  // +64: masked tail reads
   EDB_TRY(qcalc_alloc_work(q));
   s = dalloc(&T, (size_t)(amax + 1) * (amax + 1));
   if (s == EDB_OK) s = dalloc(&sigma, 64);
@@ -332,7 +332,7 @@ extern "C" edb_status edb_qcalc_genB_f32(edb_qcalc *q) {
   const int N = q->d.N;
   const long long NQ = q->p.NQ;
   const int amax = amax_of(N);
-  if (!q->B32) EDB_TRY(dalloc(&q->B32, (size_t)NQ * NQ + 64));  // +64: masked tail reads
+  if (!q->B32) EDB_TRY(dalloc(&q->B32, (size_t)c32_table_floats(N) + 64));  // +64: tail reads
   double *T = nullptr, *sigma = nullptr, *Bmm = nullptr;
   edb_status s = dalloc(&T, (size_t)(amax + 1) * (amax + 1));
   if (s == EDB_OK) s = dalloc(&sigma, 64);
@@ -365,7 +365,7 @@ long long qcalc_table_bytes(const edb_qcalc *q) {
   const long long e = q->p.NQ * q->p.NQ;
   if (q->B64) b += e * 8;
   if (q->B2) b += e * 8;
-  if (q->B32) b += e * 4 + 256;
+  if (q->B32) b += c32_table_floats(q->p.N) * 4 + 256;
   return b;
 }
 }  // namespace edb

@@ -120,6 +120,25 @@ edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const float4 *d_
 
 // Batched FP32 calQ (ALIASED): S solves, B32 the symmetric pair table in FFTW
 // order (see genB_kernel).
+//
+// The FP32 pair table keeps, per output plane k1 (FFTW order), only the l1
+// planes the batched kernel visits, l1 <= (k1 - l1) mod N: [0, k1/2] and
+// [k1+1, (k1+N)/2], at list positions p = 0 .. c32_nlist - 1.  Layout
+// [k1][p][l2][l3][k2][k3] with room for c32_maxlist planes per k1.
+__host__ __device__ inline int c32_nlist(int N, int k1) {
+  const int hi = (k1 + N) / 2 - k1;
+  return k1 / 2 + 1 + (hi > 0 ? hi : 0);
+}
+__host__ __device__ inline int c32_maxlist(int N) { return N / 2 + 1; }  // max over k1 of c32_nlist
+__host__ __device__ inline int c32_plane_pos(int N, int k1, int l1) {
+  if (l1 <= k1 / 2) return l1;
+  if (l1 > k1 && l1 <= (k1 + N) / 2) return k1 / 2 + 1 + (l1 - k1 - 1);
+  return -1;
+}
+inline long long c32_table_floats(int N) {
+  const long long NQ = (long long)N * N * N;
+  return (long long)N * c32_maxlist(N) * N * NQ;
+}
 // variant in [0, calq32_variants()) selects the solve group and CTA shape
 // (see the kernel).  C > 1 splits the l1 planes into C chunks reduced in
 // order in FP64; d_partial then holds C * S * N^3 float4.  Pair variants

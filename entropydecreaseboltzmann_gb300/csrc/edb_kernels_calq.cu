@@ -157,9 +157,10 @@ edb_status launch_calq64_reduce(const QParams &p, int nchunk, const double2 *d_p
 //
 // Work: Q^s_K = sum_L B[L][K] f^s_L f^s_((K-L) mod N) for S solves; every index
 // in FFTW order.  The terms L and M = K - L carry the same product, so B32 is
-// the symmetric pair table B[L][K] + B[M][K] written by genB_kernel (laid out
-// [l1 l2][k1][l3][k2][k3]), and only the l1 planes with l1 <= (k1 - l1) mod N
-// are summed: [0, k1/2] and [k1+1, (k1+N)/2], about half of them.
+// the symmetric pair table B[L][K] + B[M][K] written by genB_kernel, and only
+// the l1 planes with l1 <= (k1 - l1) mod N are summed: [0, k1/2] and
+// [k1+1, (k1+N)/2], about half of them.  The table holds just those planes,
+// laid out [k1][visited line][l3][k2][k3] (c32_table_floats).
 //
 // CTA = (group of SG = 2 WS solves) x (one k1, a tile of K2T k2 values, all
 // k3) x (a chunk of those l1 planes).  Thread = (solve pair {w, w+WS}, k2, run of
@@ -403,10 +404,10 @@ __device__ __forceinline__ void two_sum_fold2(u64 &hi, u64 &lo, u64 x) {
 }
 
 
-// Tensor copies (one elected thread): the B tile of line li is one 5-D box
-// {k3: N, k2: K2T, l3: N, k1: 1, line: 1} of the table, stored as
-// [line][k1][l3][k2][k3] so the tile's rows lie within N^3 floats; the f_l
-// lines of the group are one 3-D box
+// Tensor copies (one elected thread): the B tile of a line is one 5-D box
+// {k3: N, k2: K2T, l3: N, line: 1, k1: 1} of the pair table, stored as
+// [k1][visited line][l3][k2][k3] so the tile's rows lie within N^3 floats;
+// the f_l lines of the group are one 3-D box
 // {FLS floats x 2, 1 line, SG units} of the input viewed as [unit][line][l3],
 // whose columns past N*EL complex are out of bounds and land as zeros.
 __device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *tm, int c0, int c1,
@@ -429,9 +430,11 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, in
 
 // Issue (TMA: one whole warp; tensor copies from its lane 0, or one bulk copy
 // per B row and f_l line from each lane) or perform (plain: all threads) the
-// staging of the B tile and f_l line of line li into buffer `st`.
+// staging of the B tile and f_l line of line li into buffer `st`; vl is the
+// line's index in k1's visited list (its row block of the pair table).
 template <bool TMA>
-__device__ __forceinline__ void stage_line(const C32Geom &g, int li, int st, int k1, int k2_0,
+__device__ __forceinline__ void stage_line(const C32Geom &g, int li, int vl, int st, int k1,
+                                           int k2_0,
                                            int k2n, int s0, int nval, long long NQ,
                                            const float *__restrict__ B32,
                                            const float2 *__restrict__ fin, float *Bs,
@@ -440,8 +443,9 @@ __device__ __forceinline__ void stage_line(const C32Geom &g, int li, int st, int
   const int N = g.N;
   float *Bd = Bs + (size_t)st * g.BSTG;
   float2 *fd = fls + (size_t)st * g.FSTG;
-  // table layout [line][k1][l3][k2][k3]: the tile's rows l3 are N^2 apart
-  const float *Bsrc = B32 + ((long long)li * N + k1) * NQ + (long long)k2_0 * N;
+  // table layout [k1][visited line][l3][k2][k3]: the tile's rows l3 are N^2 apart
+  const float *Bsrc =
+      B32 + ((long long)k1 * c32_maxlist(N) * N + vl) * NQ + (long long)k2_0 * N;
   const long long NN = (long long)N * N;
   const int EL = g.EL;  // s0 / nval count data units of EL float2 per element
   const float2 *fsrc = fin + ((long long)s0 * NQ + (long long)li * N) * EL;
@@ -450,7 +454,7 @@ __device__ __forceinline__ void stage_line(const C32Geom &g, int li, int st, int
     if ((threadIdx.x & 31) == 0) {
       mbar_expect_tx(full + st, (uint32_t)(N * g.K2T * N * 4 + g.SG * g.FLS * 8));
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      tma_load_5d(Bd, tmB, 0, k2_0, 0, k1, li, full + st);
+      tma_load_5d(Bd, tmB, 0, k2_0, 0, vl, k1, full + st);
       tma_load_3d(fd, tmF, 0, li, s0, full + st);
     }
     __syncwarp(warp_mask());
@@ -724,7 +728,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
   // l1 = plane_l1(p).  This chunk takes list entries [P0, P1) and walks their
   // l-lines j = 0 .. nlines - 1 (line j: plane P0 + j / N, l2 = j mod N).
   const int plo = k1 / 2;
-  const int nlist = plo + 1 + max(0, (k1 + N) / 2 - k1);
+  const int nlist = c32_nlist(N, k1);
   auto plane_l1 = [&](int p) { return p <= plo ? p : k1 + 1 + (p - plo - 1); };
   const int PPC = (nlist + C - 1) / C;
   const int P0 = min(nlist, chunk * PPC), P1 = min(nlist, P0 + PPC);
@@ -775,7 +779,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
   int jstop = nlines;   // first line not finished by every warp (abort drain)
   if (TMA && warp == 0 && nlines > 0) {
     for (int j = 0; j < NST - 1 && j < nlines; ++j)
-      stage_line<true>(g, line_li(j), j % NST, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls,
+      stage_line<true>(g, line_li(j), P0 * N + j, j % NST, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls,
                        full, tmap, &tmB, &tmF);
     stage_plane<true>(g, (k1 - plane_l1(P0) + N) % N, u0, nval, NQ, fin, plb, &pbar[0]);
     ++planes;
@@ -823,13 +827,14 @@ __global__ void __launch_bounds__(MAXT, MINB)
       if (warp == jn % nfull && jn < nlines) {
         const int sn = jn % NST;
         if (j >= 1) mbar_wait(&empty[sn], (uint32_t)(((j - 1) / NST) & 1), to);
-        stage_line<true>(g, line_li(jn), sn, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full,
+        stage_line<true>(g, line_li(jn), P0 * N + jn, sn, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full,
                          tmap, &tmB, &tmF);
       }
       mbar_wait(&full[st], (uint32_t)((j / NST) & 1), to);
     } else {
       __syncthreads();  // previous line's readers are done (single buffer)
-      stage_line<false>(g, li, st, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full, tmap, &tmB, &tmF);
+      stage_line<false>(g, li, P0 * N + j, st, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full,
+                        tmap, &tmB, &tmF);
       __syncthreads();
     }
 
@@ -1104,11 +1109,12 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   if (tma && 2 * c32_geom(N, A, K2T, 1, 1, 0, units, el, true).FLS <= 256 && N <= 256) {
     const int FLS = c32_geom(N, A, K2T, 1, 1, 0, units, el, true).FLS;
     const long long NQ = (long long)N * N * N;
-    const cuuint64_t bdim[5] = {(cuuint64_t)N, (cuuint64_t)N, (cuuint64_t)N, (cuuint64_t)N,
-                                (cuuint64_t)N * N};
+    // pair table [k1][visited line][l3][k2][k3]: dims k3, k2, l3, visited line, k1
+    const long long VL = (long long)c32_maxlist(N) * N;
+    const cuuint64_t bdim[5] = {(cuuint64_t)N, (cuuint64_t)N, (cuuint64_t)N, (cuuint64_t)VL,
+                                (cuuint64_t)N};
     const cuuint64_t bstr[4] = {(cuuint64_t)N * 4, (cuuint64_t)N * N * 4, (cuuint64_t)NQ * 4,
-                                (cuuint64_t)N * NQ * 4};
-    // table [line][k1][l3][k2][k3]: dims k3, k2, l3, k1, line
+                                (cuuint64_t)(VL * NQ * 4)};
     const cuuint32_t bbox[5] = {(cuuint32_t)N, (cuuint32_t)K2T, (cuuint32_t)N, 1, 1};
     const long long nunits = vr.pair ? (S + 1) / 2 : S;
     const cuuint64_t fdim[3] = {(cuuint64_t)N * 2 * el, (cuuint64_t)N * N, (cuuint64_t)nunits};

@@ -219,9 +219,10 @@ edb_status launch_bmm(int N, double gamma, double L, int filter, int mode, const
 // One CTA per row l (centred); columns k over all N^3 centred modes.
 // Writes B64[l][k] (when given) and, when B32 is given, the symmetric pair
 // table of the batched kernel in FFTW order (lf = (l - n) mod N per
-// dimension), laid out [l1 l2][k1][l3][k2][k3]: the terms l and m = k - l of
-// a Q-hat sum carry the same product f_l f_m, so the batched kernel visits
-// only the l1 planes with l1 <= m1 and weights them by B[l][k] + B[m][k], computed here in
+// dimension), for the visited planes only (c32_plane_pos): the terms l and
+// m = k - l of a Q-hat sum carry the same product f_l f_m, so the batched
+// kernel visits only the l1 planes with l1 <= m1 and weights them by
+// B[l][k] + B[m][k], computed here in
 // FP64 and rounded once; on the planes l1 = m1 (both terms inside the plane)
 // the entry stays B[l][k].  The partner's value needs no second table lookup:
 // l + m and |l - m| are the same for both, so B[m][k] differs from B[l][k]
@@ -256,14 +257,18 @@ __global__ void genB_kernel(int N, int filter, double rval, const double *__rest
     const double t = T[(long long)a * W + b];
     double v = t * sigmal * sigmam * rval - Bmm[m];
     if (B64) B64[lc * NQ + kc] = v;
-    if (B32) {
-      // [line][k1][l3][k2][k3] in FFTW order (line = l1 N + l2): the batched
-      // kernel's tile for one line and k1 lies within N^3 floats
-      const long long k1f = (k1 - n + N) % N;
+    const int k1f = (k1 - n + N) % N;
+    const int pos = B32 ? c32_plane_pos(N, k1f, (int)(lf / (N * N))) : -1;
+    if (pos >= 0) {
+      // [k1][p][l2][l3][k2][k3] (FFTW order; p = position of l1 in k1's
+      // visited list): the batched kernel's tile for one line and k1 lies
+      // within N^3 floats, and planes it never visits are not stored
       const long long k23 = (long long)((k2 - n + N) % N) * N + (k3 - n + N) % N;
+      const long long l2f = (lf / N) % N, l3f = lf % N;
       double w = v;
       if (l1 != m1) w += t * sigmam * sigmal * rval - Bmm[lc];  // B[m][k], as its row writes it
-      B32[((lf / N * N + k1f) * N + lf % N) * (N * N) + k23] = (float)w;
+      B32[((((long long)k1f * c32_maxlist(N) + pos) * N + l2f) * N + l3f) * (N * N) + k23] =
+          (float)w;
     }
   }
 }

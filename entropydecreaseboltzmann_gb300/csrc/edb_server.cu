@@ -146,10 +146,8 @@ long long slot_bytes(const edb_server *s, int N) {
          (long long)sizeof(EfixState) + 48;
 }
 
-long long table_bytes_of(int N) {
-  const long long NQ = (long long)N * N * N;
-  return NQ * NQ * 4 + 256;
-}
+// The FP32 pair table of edb_qcalc_genB_f32 (visited planes only).
+long long table_bytes_of(int N) { return c32_table_floats(N) * 4 + 256; }
 
 long long fixed_bytes_of(int N) {
   const long long NQ = (long long)N * N * N;

@@ -117,9 +117,10 @@ def test_continuous_admission_and_budget(edb):
     st = srv.stats()
     assert st["completed"] == 2 and st["tts_p50_s"] <= st["tts_p99_s"]
     srv.close()
-    # a budget of one table (N^6 x 4 B = 11.9 MB), its transfer staging
-    # (64 x N^3 x 40 B = 4.4 MB) and about 17 slots (N^3 x 248 B each: RK4
-    # stages plus 8 chunk partial sums), so the 70 requests are served in waves
+    # a budget of one table (the FP32 pair table: N (N/2 + 1) N^4 x 4 B =
+    # 7.0 MB), its transfer staging (64 x N^3 x 40 B = 4.4 MB) and about 29
+    # slots (N^3 x 248 B each: RK4 stages plus 8 chunk partial sums), so the 70
+    # requests are served in waves
     srv = edb.Server(hbm_budget_bytes=2.4e7, scheme=edb.SCHEME_RK4, dt=0.01)
     for j in range(70):
         srv.submit(N, 0.0, R, 3, f)
