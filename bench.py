@@ -390,7 +390,7 @@ def main():
             "data": "synthetic (seeded BKW + Gaussian bump, mass 1)",
             "config": {"workload": WORKLOAD, "solves": S, "N": N, "L": L_BOX, "scheme": "RK4",
                        "dt": DT, "evals_per_step": evals_per_step,
-                       "l2": "inputs larger than L2 (B32 764 MB, FP64 state 906 MB); no flush",
+                       "l2": "inputs larger than L2 (FP32 pair table 414 MB, FP64 state 906 MB); no flush",
                        "parallelism": f"replicas x{ws}"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
