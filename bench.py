@@ -3,27 +3,34 @@
 Workload (one GPU): the uniform batch of 4096 independent solves at N = 24,
 L = 7, Maxwell molecules (gamma = 0, filter off, ALIASED index mode), all
 sharing one kernel table; BKW initial data at seeded t0 ~ U[5.5, 8] plus a
-Gaussian bump, mass renormalised to 1; RK4 with dt = 0.01.  One step = one
-RK4 step of every solve = 4 x 4096 Q-hat evaluations, each N^6 = 1.91e8 terms.
+Gaussian bump, mass renormalised to 1; RK4 with dt = 0.01, with the FP64
+inverse transform, entropy and EntropyFix rule after every step.  One step =
+one RK4 step of every solve = 4 x 4096 Q-hat evaluations, each N^6 = 1.91e8
+terms.
 
 value: Q-hat evaluations/s with the state resident in HBM (device-timed,
 CUDA events on the launching stream).  e2e: the same metric through the C ABI
 with host buffers — per step, edb_batch_load (pinned host real-space f in,
 forward FFT), one RK4 step, edb_batch_read (inverse FFT, real-space f out).
 Also reported: the FP64 drop-in single-solve path at N = 24 and N = 32
-(evals/s and B-stream bandwidth), the BKW L-infinity error of the batched
-FP32 path after 50 RK4 steps, the roofline of the dominant kernel, the
-CPU baseline (the oracle's restatement of QCalculator::calQ on host threads)
-and the serving engine on the serving-stream mix (N in {16, 24, 32} with
-probabilities 0.5/0.3/0.2, gamma in {0, 1}, horizons log-uniform in [20, 500]
-RK4 steps, 5% BKW requests, 80 GB budget): its capacity (all requests at
-once) and p50/p99 time-to-solution under Poisson arrivals at 70% of that
-capacity.  --uneven adds the uneven batch (512 solves each at N = 16, 24,
-32, gamma in {0, 0.5, 1}, SSP3 dt = 0.005, U{20..200} steps).
+(evals/s and B-stream bandwidth), the BKW L-infinity error after every step
+of the batched FP32 path (50 RK4 steps) and of the FP64 testBKW3D case
+(N = 16, L = 6, 100 RK4 steps; odd companions N = 17, 21, 25), the roofline
+of the dominant kernel, the CPU baseline (the oracle's restatement of
+QCalculator::calQ on host threads), the serving engine on the serving-stream
+mix (N in {16, 24, 32} with probabilities 0.5/0.3/0.2, gamma in {0, 1},
+horizons log-uniform in [20, 500] RK4 steps, 5% BKW requests, 80 GB budget):
+its capacity (requests in flight) and p50/p99 time-to-solution under Poisson
+arrivals at 70% of that capacity for 60 s, and the uneven batch (512 solves
+each at N = 16, 24, 32, gamma in {0, 0.5, 1}, SSP3 dt = 0.005, U{20..200}
+steps).
 
 Usage:  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+        python bench.py --probe calq32|calq64 [--probe-N N] [--probe-S S] ...
 For N > 1 (torchrun) every rank runs an independent replica of the workload
 (the solves are independent: replicas only, no collective on the data path).
+--probe runs one hot kernel on a small fixed case (the command the ncu
+captures in profiles/ run) and prints its per-launch time.
 """
 from __future__ import annotations
 
@@ -129,10 +136,23 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def make_batch_inputs(S, seed=1002):
-    from entropydecreaseboltzmann_gb300 import data
+def data_module():
+    """The seeded initial-data helpers (numpy only), loaded by path so that
+    the reference arm never imports the package (which loads libedb.so)."""
+    import importlib.util
 
-    F0, t0, amp = data.bkw_bump_batch(S, N_MODES, L_BOX, seed)
+    if "edb_bench_data" in sys.modules:
+        return sys.modules["edb_bench_data"]
+    path = os.path.join(ROOT, "entropydecreaseboltzmann_gb300", "data.py")
+    spec = importlib.util.spec_from_file_location("edb_bench_data", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    sys.modules["edb_bench_data"] = mod
+    return mod
+
+
+def make_batch_inputs(S, seed=1002):
+    F0, t0, amp = data_module().bkw_bump_batch(S, N_MODES, L_BOX, seed)
     return F0, t0, amp
 
 
@@ -163,19 +183,28 @@ def cpu_baseline(seconds=12.0, threads=None):
 
 
 def run_reference_arm(args):
+    """The reference's CPU path on this host's cores: the oracle's
+    restatement of QCalculator::calQ (the reference's loops; ALIASED index
+    mode) inside BKW3D::RK4's step (BKW.h:480-510: four calQ, the stage
+    updates, then ifft, calEntropy and the fix rule), one independent solve
+    per host thread.  Imports nothing from the package."""
     ws, rank, local = dist_env()
     if rank != 0:
         return 0
-    from oracle.oracle import INDEX_ALIASED, Oracle, build_oracle
+    from oracle.oracle import INDEX_ALIASED, EntropyFixOracle, Oracle, build_oracle
 
     build_oracle()
     o = Oracle()
     threads = os.cpu_count() or 1
     N = N_MODES
+    NQ = N ** 3
     B = o.genB(N, 0.0, L_BOX, False, INDEX_ALIASED)
     F0, _, _ = make_batch_inputs(threads, seed=1002)
     fh = np.fft.fftn(F0.reshape(threads, N, N, N), axes=(1, 2, 3)).reshape(threads, -1)
     dt = DT
+    efix = [EntropyFixOracle(o, NQ) for _ in range(threads)]
+    H_prev = [1.0] * threads
+    step_no = [0]
 
     def rk4_step(fh):
         # BKW.h:481-494 on `threads` independent solves, each calQ on its own thread
@@ -183,7 +212,18 @@ def run_reference_arm(args):
         q1 = o.calQ_batch(N, B, fh + 0.5 * dt * q0, INDEX_ALIASED, nthreads=threads)
         q2 = o.calQ_batch(N, B, fh + 0.5 * dt * q1, INDEX_ALIASED, nthreads=threads)
         q3 = o.calQ_batch(N, B, fh + dt * q2, INDEX_ALIASED, nthreads=threads)
-        return fh + dt / 6.0 * (q0 + 2.0 * q1 + 2.0 * q2 + q3)
+        fh = fh + dt / 6.0 * (q0 + 2.0 * q1 + 2.0 * q2 + q3)
+        # BKW.h:497-510: ifft, calEntropy, the fix rule on Re F
+        for s in range(threads):
+            F = o.fft3d(N, fh[s], inverse=True)
+            H = o.calentropy(N, L_BOX, F)
+            if step_no[0] and H - H_prev[s] > 1.0e-10:
+                f = np.ascontiguousarray(F.real)
+                efix[s].FixSol(f, H_prev[s] / (2.0 * L_BOX) ** 3)
+                H = o.calentropy(N, L_BOX, f.astype(np.complex128))
+            H_prev[s] = H
+        step_no[0] += 1
+        return fh
 
     for _ in range(args.warmup):
         fh = rk4_step(fh)
@@ -193,18 +233,21 @@ def run_reference_arm(args):
     el = time.perf_counter() - t0
     evals = 4 * threads * args.steps
     value = evals / el
+    sample = (f"{threads} solves x {args.steps} RK4 steps (4 calQ each, then ifft, entropy and "
+              "the fix rule) of the 4096-solve N=24 workload, one solve per host thread; the "
+              "reference's C++ is not on the GPU host (its sources are not there, and its "
+              "x86 build does not run on Arm), so the oracle's restatement of the same loops "
+              "is timed")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": WORKLOAD + f" (CPU sample: {threads} of the 4096 solves per step)",
-                                        "cpu_threads": threads},
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD + ", fix on" +
+                   f" (CPU sample: {threads} of the 4096 solves per step; the metric is a "
+                   "per-evaluation rate)", "cpu_threads": threads},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{threads} solves x {args.steps} RK4 steps (4 calQ each) of "
-                                   "the 4096-solve N=24 workload, one solve per host thread; the "
-                                   "reference's C++ cannot be built on the GPU host (its sources "
-                                   "are not there), so the oracle's restatement of "
-                                   "QCalculator::calQ (same loops) is timed"},
+                         "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -223,13 +266,26 @@ def main():
                     help="request pool of the capacity run (0: skip serving)")
     ap.add_argument("--serve-capacity-seconds", type=float, default=20.0,
                     help="window of the steady-state capacity run")
-    ap.add_argument("--serve-seconds", type=float, default=20.0,
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="arrival window of the Poisson run")
-    ap.add_argument("--uneven", action="store_true", help="also run the uneven batch")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven batch")
     ap.add_argument("--uneven-per-n", type=int, default=512)
+    ap.add_argument("--probe", choices=["calq32", "calq64"], default=None,
+                    help="run one hot kernel on a small fixed case (see probe())")
+    ap.add_argument("--probe-N", type=int, default=24)
+    ap.add_argument("--probe-S", type=int, default=256)
+    ap.add_argument("--probe-L", type=float, default=7.0)
+    ap.add_argument("--probe-mode", type=int, default=1, help="calq64: index mode")
+    ap.add_argument("--probe-reps", type=int, default=2)
+    ap.add_argument("--probe-variant", type=int, default=-1,
+                    help="calq32: this kernel variant instead of the autotuned one")
+    ap.add_argument("--probe-sweep", action="store_true",
+                    help="calq32: time every kernel variant (no chunks and 8 chunks)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.probe:
+        return probe(args)
 
     import torch
 
@@ -261,7 +317,9 @@ def main():
     q = edb.QCalculator(N, 0, L=L_BOX, filter=False, index_mode=edb.INDEX_ALIASED)
     q.genB()
     F0, t0s, _ = make_batch_inputs(S, seed=1002 + rank)
-    bs = edb.BatchSolver(q, S, L_BOX, edb.SCHEME_RK4, DT)
+    # every step: four batched Q-hat stages, the FP64 stage updates, then the
+    # FP64 inverse transform, entropy and the EntropyFix rule (BKW.h:480-510)
+    bs = edb.BatchSolver(q, S, L_BOX, edb.SCHEME_RK4, DT, fix_entropy=True)
     d_F0 = torch.from_numpy(F0).cuda()
     bs.load_device(d_F0, stream)
     torch.cuda.synchronize()
@@ -315,7 +373,7 @@ def main():
     bs.step(1)
     _ = bs.read(real=True)
     torch.cuda.synchronize()
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = args.steps
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         bs.load(h_in.numpy())
@@ -364,21 +422,26 @@ def main():
             kind["hbm_frac"] = kind["B_stream_GBs"] / peaks["hbm_gbs"]
             kind["hbm_frac_read"] = kind["B_read_GBs"] / peaks["hbm_gbs"]
 
-    # ---- BKW accuracy of the batched FP32 path (50 RK4 steps, pure BKW solves)
+    # ---- BKW accuracy of the batched FP32 path (50 RK4 steps, pure BKW
+    # solves, fix on as in the timed region): L-inf after every step
     Sb = 32
     t0b = np.linspace(5.5, 8.0, Sb)
     fb = np.stack([data.bkw_grid(N, L_BOX, t) for t in t0b])
-    bb = edb.BatchSolver(q, Sb, L_BOX, edb.SCHEME_RK4, DT)
+    bb = edb.BatchSolver(q, Sb, L_BOX, edb.SCHEME_RK4, DT, fix_entropy=True)
     bb.load(fb)
-    bb.step(50)
-    fend = bb.read(real=True)
-    exact = np.stack([data.bkw_grid(N, L_BOX, t + 50 * DT) for t in t0b])
-    bkw_linf = float(np.max(np.abs(fend - exact)))
+    bkw_by_step = []
+    for st in range(1, 51):
+        bb.step(1)
+        f = bb.read(real=True)
+        exact = np.stack([data.bkw_grid(N, L_BOX, t + st * DT) for t in t0b])
+        bkw_by_step.append(float(np.max(np.abs(f - exact))))
+    bkw_linf = max(bkw_by_step)
 
     del bb, bs
     torch.cuda.synchronize()
+    cfg1 = run_config1(edb, data)
     serve = run_serving(edb, args, rank) if args.serve_requests > 0 else None
-    uneven = run_uneven(edb, args, rank) if args.uneven else None
+    uneven = None if args.no_uneven else run_uneven(edb, args, rank)
 
     line = None
     if rank == 0:
@@ -388,7 +451,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32c (complex FP32, compensated sums; FP64 state)",
             "data": "synthetic (seeded BKW + Gaussian bump, mass 1)",
-            "config": {"workload": WORKLOAD, "solves": S, "N": N, "L": L_BOX, "scheme": "RK4",
+            "config": {"workload": WORKLOAD + ", FP64 ifft + entropy + EntropyFix rule every step",
+                       "solves": S, "N": N, "L": L_BOX, "scheme": "RK4", "fix_entropy": True,
                        "dt": DT, "evals_per_step": evals_per_step,
                        "l2": "inputs larger than L2 (FP32 pair table 414 MB, FP64 state 906 MB); no flush",
                        "parallelism": f"replicas x{ws}"},
@@ -420,6 +484,8 @@ def main():
             "batched_over_plain_fp64_N24": value / fp64["N24"]["native"]["evals_per_s"],
             "batched_over_fp64_dropin_N24": value / fp64["N24"]["emulated"]["evals_per_s"],
             "bkw_linf_fp32_50_steps": bkw_linf,
+            "bkw_linf_fp32_by_step": bkw_by_step,
+            "bkw_fp64_config1": cfg1,
             "serve": serve,
             "cpu_baseline": cpu,
         }
@@ -429,6 +495,99 @@ def main():
     if pg is not None:
         pg.barrier()
         pg.destroy_process_group()
+    return 0
+
+
+def probe(args):
+    """One hot kernel on a small fixed case, the command the ncu captures in
+    profiles/ run:
+      --probe calq32: batched FP32 Q-hat of --probe-S BKW solves (ALIASED
+        table, L = --probe-L), the autotuned variant or --probe-variant;
+        --probe-sweep times every variant with 1 and 8 chunks first;
+      --probe calq64: FP64 drop-in Q-hat of one BKW solve (index mode
+        --probe-mode).
+    Prints the per-launch time from CUDA events (not meaningful under ncu)."""
+    import ctypes as C
+
+    import torch
+
+    import entropydecreaseboltzmann_gb300 as edb
+    from entropydecreaseboltzmann_gb300 import data
+
+    N, S, L = args.probe_N, args.probe_S, args.probe_L
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    if args.probe == "calq32":
+        q = edb.QCalculator(N, 0, L=L, filter=False, index_mode=edb.INDEX_ALIASED)
+        q.genB()
+        F0, _, _ = data.bkw_bump_batch(S, N, L, seed=5)
+        fh = np.fft.fftn(F0.reshape(S, N, N, N), axes=(1, 2, 3)).reshape(S, -1)
+        fin = torch.from_numpy(fh.astype(np.complex64)).cuda()
+        out = torch.empty_like(fin)
+        if args.probe_sweep:
+            part = torch.empty(8 * S * N ** 3 * 4, dtype=torch.float32, device="cuda")
+            for Cn in (1, 8):
+                first = None
+                for var in range(edb.lib.edb_qcalc_batch_variants()):
+                    try:
+                        q.calQ_batch_f32_ex(S, var, Cn, part, fin, out, stream)
+                    except edb.EdbError as e:
+                        if e.status == 1 and var > 0:
+                            continue
+                        raise
+                    torch.cuda.synchronize()
+                    if first is None:
+                        first = out.clone()
+                    same = bool(torch.equal(out.view(torch.float32), first.view(torch.float32)))
+                    a0 = torch.cuda.Event(enable_timing=True)
+                    a1 = torch.cuda.Event(enable_timing=True)
+                    a0.record(stream)
+                    for _ in range(args.probe_reps):
+                        q.calQ_batch_f32_ex(S, var, Cn, part, fin, out, stream)
+                    a1.record(stream)
+                    torch.cuda.synchronize()
+                    t = a0.elapsed_time(a1) / args.probe_reps
+                    print(f"variant {var} chunks {Cn}: {t:.3f} ms, "
+                          f"{10 * float(N) ** 6 * S / (t * 1e-3) / 1e12:.2f} TFLOP/s, "
+                          f"bits {'same' if same else 'DIFFER'}")
+                del first
+            del part
+        if args.probe_variant >= 0:
+            def run():
+                q.calQ_batch_f32_ex(S, args.probe_variant, 1, None, fin, out, stream)
+        else:
+            print(f"autotuned variant {q.autotune_batch(S, fin, out, stream)}")
+
+            def run():
+                q.calQ_batch_f32(S, fin, out, stream)
+        terms = float(N) ** 6 * S
+    else:
+        q = edb.QCalculator(N, 0, L=L, filter=False, index_mode=args.probe_mode)
+        q.genB()
+        f = data.bkw_grid(N, L, 5.5)
+        fin = torch.from_numpy(np.fft.fftn(f.reshape(N, N, N)).reshape(-1)).cuda()
+        out = torch.empty_like(fin)
+
+        def run():
+            q.calQ_device(fin, out, stream)
+        terms = float(q.info()["terms"])
+    run()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.probe_reps):
+        run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.probe_reps
+    st = edb.device_status(clear=True)
+    print(f"device status {st}, finite {bool(torch.isfinite(torch.view_as_real(out)).all())}")
+    p1, p2 = C.c_double(), C.c_double()
+    edb.lib.edb_measure_fp32_peak(C.byref(p1))
+    edb.lib.edb_measure_fp32x2_peak(C.byref(p2))
+    print(f"FP32 FMA peak probe: scalar {p1.value:.1f} TFLOP/s, packed f32x2 {p2.value:.1f} TFLOP/s")
+    print(f"{args.probe} N={N} S={S}: {ms:.3f} ms/launch, "
+          f"{10 * terms / (ms * 1e-3) / 1e12:.2f} TFLOP/s (10 flop/term)")
     return 0
 
 
@@ -477,6 +636,32 @@ def run_serving(edb, args, rank):
                  f"p50/p99 are reported at a sustained 70% of the measured capacity"),
     }
     out.update({k: st[k] for k in SERVE_KEYS})
+    return out
+
+
+def run_config1(edb, data):
+    """The testBKW3D case on RK4 through the FP64 device-resident integrator:
+    N = 16 on [-6, 6]^3, BKW initial data at t0 = 5.5, dt = 0.01, 100 steps,
+    ALIASED index mode with L = 6 in the kernel scale and the filter off; L-inf
+    of Re F against the exact BKW solution after every step.  The odd
+    companions N = 17, 21, 25 show how the discretisation floor falls with N
+    (L-inf after every step, reported as the maximum and the final value)."""
+    dt, steps, L = 0.01, 100, 6.0
+    out = {"workload": "N=16, L=6, BKW t0=5.5, RK4 dt=0.01 x 100 steps, FP64, aliased, filter off"}
+    for N in (16, 17, 21, 25):
+        b = edb.BKW3D(N, L, L=L, filter=False, index_mode=edb.INDEX_ALIASED, record_F=True)
+        b.setInitial(data.bkw_grid(N, L, 5.5))
+        t0 = time.perf_counter()
+        b.RK4(0.0, (steps - 0.5) * dt, dt)
+        wall = time.perf_counter() - t0
+        linf = [float(np.max(np.abs(b.F_history[s] - data.bkw_grid(N, L, 5.5 + (s + 1) * dt))))
+                for s in range(b.nsteps)]
+        rec = {"steps": b.nsteps, "linf_max": max(linf), "linf_final": linf[-1],
+               "wall_s_with_genB": wall}
+        if N == 16:
+            rec["linf_by_step"] = linf
+        out[f"N{N}"] = rec
+        del b
     return out
 
 

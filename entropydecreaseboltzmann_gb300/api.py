@@ -19,10 +19,18 @@ from ._lib import (INDEX_REFERENCE, R_REFERENCE, SCHEME_CFE, SCHEME_DUFORT, SCHE
 
 
 def device_status(clear: bool = True) -> int:
-    """Nonzero when a bounded wait inside the batched kernel ran out."""
+    """Nonzero when a bounded wait inside a Q-hat kernel ran out (bit 0: the
+    batched kernel, bit 1: the double-float FP64 kernel)."""
     v = C.c_int()
     check(lib.edb_device_status(C.byref(v), int(clear)))
     return v.value
+
+
+def set_wait_limit_ns(ns: int) -> None:
+    """Limit of each bounded wait inside the Q-hat kernels in nanoseconds
+    (ns < 0: the 200 ms default; 0: every wait runs out at once).  For tests
+    of the timeout path."""
+    check(lib.edb_set_wait_limit_ns(int(ns)))
 
 
 def kernel_launch_count() -> int:

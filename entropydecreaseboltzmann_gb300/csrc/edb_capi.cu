@@ -17,6 +17,24 @@ namespace edb {
 
 static thread_local std::string g_err;
 static std::atomic<long long> g_launches{0};
+static constexpr unsigned long long kDefaultWaitNs = 200000000ull;  // 200 ms
+static std::atomic<unsigned long long> g_wait_ns{kDefaultWaitNs};
+
+unsigned long long wait_limit_ns() { return g_wait_ns.load(std::memory_order_relaxed); }
+
+// After a synchronous call's work has finished: EDB_ETIMEDOUT (and the words
+// cleared) when a bounded wait inside a Q-hat kernel ran out, whose output is
+// then invalid.
+static edb_status check_device_waits(const char *what) {
+  int a = 0, b = 0;
+  EDB_TRY(read_calq32_status(&a, true));
+  EDB_TRY(read_calq64x_status(&b, true));
+  if (a || b)
+    return fail(EDB_ETIMEDOUT, std::string(what) +
+                                   ": a bounded wait inside a Q-hat kernel ran out; the "
+                                   "result is invalid");
+  return EDB_OK;
+}
 
 void set_error(const std::string &msg) { g_err = msg; }
 edb_status fail(edb_status s, const std::string &msg) {
@@ -28,6 +46,19 @@ edb_status cuda_fail(cudaError_t e, const char *what) {
   return EDB_ECUDA;
 }
 void count_launch(int n) { g_launches += n; }
+
+int device_sm_count() {
+  constexpr int kMaxDev = 64;
+  static std::atomic<int> cache[kMaxDev];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return 1;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v > 0) return v;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v < 1)
+    return 1;
+  cache[dev].store(v, std::memory_order_relaxed);
+  return v;
+}
 
 edb_status ensure_device() {
   int n = 0;
@@ -249,7 +280,8 @@ static edb_status qcalc_tune_fp64(edb_qcalc *q) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   q->c64x_minb = best_minb;
-  return rc;
+  if (rc != EDB_OK) return rc;
+  return check_device_waits("genB (FP64 kernel timing)");
 }
 
 extern "C" edb_status edb_qcalc_genB(edb_qcalc *q) {
@@ -438,7 +470,7 @@ extern "C" edb_status edb_qcalc_calQ(edb_qcalc *q, const double *fin, double *Qo
   EDB_TRY(qcalc_fp64(q, q->fin, q->Q, q->st));
   EDB_CUDA(cudaMemcpyAsync(Qout, q->Q, bytes, cudaMemcpyDeviceToHost, q->st));
   EDB_CUDA(cudaStreamSynchronize(q->st));
-  return EDB_OK;
+  return check_device_waits("calQ");
 }
 
 extern "C" edb_status edb_qcalc_calQ_batch_f32_device(edb_qcalc *q, int S, const float *d_fin,
@@ -536,7 +568,16 @@ extern "C" edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float 
 
 extern "C" edb_status edb_device_status(int *status, int clear) {
   if (!status) return fail(EDB_EINVAL, "null output");
-  return read_calq32_status(status, clear != 0);
+  int a = 0, b = 0;
+  EDB_TRY(read_calq32_status(&a, clear != 0));
+  EDB_TRY(read_calq64x_status(&b, clear != 0));
+  *status = (a ? 1 : 0) | (b ? 2 : 0);
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_set_wait_limit_ns(long long ns) {
+  g_wait_ns.store(ns < 0 ? kDefaultWaitNs : (unsigned long long)ns, std::memory_order_relaxed);
+  return EDB_OK;
 }
 
 // ===================================================================== fft3d
@@ -623,7 +664,7 @@ extern "C" edb_status edb_efix_destroy(edb_efix *e) {
 
 static edb_status efix_check(edb_efix *e, int Nf, const double *f) {
   if (!e || !f) return fail(EDB_EINVAL, "null argument");
-  // the reference asserts Nf == Nt (EntropyFix.h:124, 183, 270)
+  // the reference asserts Nf == Nt (EntropyFix.h:68, 127, 214)
   if (Nf != e->Nt) return fail(EDB_EINVAL, "Nf must equal Nt");
   return EDB_OK;
 }
@@ -937,7 +978,7 @@ extern "C" edb_status edb_solver_run(edb_solver *s, double T0, double TEnd, doub
   EDB_CUDA(cudaStreamSynchronize(st));
   s->trace_n = total;
   if (nsteps) *nsteps = total;
-  return EDB_OK;
+  return check_device_waits("solver run");
 }
 
 extern "C" edb_status edb_solver_get(edb_solver *s, double *Fhat, double *F) {
@@ -1274,7 +1315,10 @@ extern "C" edb_status edb_batch_step(edb_batch *b, int nsteps, void *stream) {
     EDB_CUDA(cudaGraphLaunch(b->exec, st));
     count_launch(b->launches_per_step);
   }
-  if (!stream) EDB_CUDA(cudaStreamSynchronize(st));
+  if (!stream) {
+    EDB_CUDA(cudaStreamSynchronize(st));
+    return check_device_waits("batch step");
+  }
   return EDB_OK;
 }
 

@@ -38,6 +38,9 @@ void count_launch(int n = 1);
   } while (0)
 
 edb_status ensure_device();
+// Streaming multiprocessors of the current device (queried once per device;
+// 1 if the query fails).  Launch sizing uses it instead of a fixed count.
+int device_sm_count();
 
 // Device allocation of `count` elements of T (EDB_ENOMEM on failure).
 template <typename T>
@@ -150,9 +153,13 @@ size_t calq32_pair_bytes(int N, int S);
 edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin,
                                float2 *d_Q, cudaStream_t st, int variant, int C = 1,
                                float4 *d_partial = nullptr, float4 *d_pairs = nullptr);
-// Reads (and optionally clears) the batched kernel's status word: nonzero
-// when a bounded wait inside it ran out.
+// Reads (and optionally clears) the batched kernel's / the double-float FP64
+// kernel's status word: nonzero when a bounded wait inside it ran out.
 edb_status read_calq32_status(int *status, bool clear);
+edb_status read_calq64x_status(int *status, bool clear);
+// Limit of every bounded mbarrier wait of the Q-hat kernels, passed to each
+// launch (default 200 ms; see edb_set_wait_limit_ns).
+unsigned long long wait_limit_ns();
 
 // Batched cubic DFT (FP64 or FP32), out-of-place; d_tmp holds batch*N^3 complex.
 edb_status launch_dft3d(int N, int batch, const void *d_in, void *d_out, void *d_tmp,

@@ -40,7 +40,7 @@ static const int CALQ64_THREADS = 256;
 
 int calq64_nchunk(const QParams &p) {
   long long tiles = (p.KC + CALQ64_THREADS - 1) / CALQ64_THREADS;
-  long long want = (4LL * 152 + tiles - 1) / tiles;
+  long long want = (4LL * device_sm_count() + tiles - 1) / tiles;
   if (want < 1) want = 1;
   if (want > 64) want = 64;
   if (want > p.NQ) want = p.NQ;
@@ -206,7 +206,9 @@ constexpr int ROWPAD = 8;                 // floats after each B-tile row
 constexpr int FLPAD = 2;                  // complex after each f_l line
 constexpr int PLPAD = 2;                  // complex after each solve's plane
 constexpr int FOLD_LINES = 4;             // l-lines per compensated fold
-constexpr unsigned long long WAIT_LIMIT_NS = 200000000ull;  // 200 ms per mbarrier wait
+// Limit of the drain after a wait ran out: the block then waits this long at
+// most for each copy it issued, so none lands after it exits.
+constexpr unsigned long long DRAIN_LIMIT_NS = 1000000000ull;
 
 __device__ int g_calq32_status;  // nonzero: a bounded wait ran out
 
@@ -221,7 +223,9 @@ struct C32Geom {
 // Shared-memory layout for a CTA: NST stages of (B tile, f_l lines), NPL
 // m1-planes and, when HLT > 0, the compensated (hi, lo) sums of HLT threads
 // (2 * A * SC packed pairs each, thread-fastest so accesses never conflict).
-// Barriers: full[MAX_ST], empty[MAX_ST], plane[2].  SG data units (solves, or
+// The first 128 bytes: barriers full[MAX_ST], empty[MAX_ST], plane[2] (80 B),
+// then the fill count of each stage, int[MAX_ST] (the abort drain waits for
+// each stage's last fill).  SG data units (solves, or
 // solve pairs) of EL float2 per element (1: (re, im); 2: (re_a, re_b),
 // (im_a, im_b) of a pair).
 __host__ __device__ inline C32Geom c32_geom(int N, int A, int K2T, int NST, int NPL, int HLT,
@@ -249,7 +253,7 @@ __host__ __device__ inline C32Geom c32_geom(int N, int A, int K2T, int NST, int 
     g.FLS = (g.RA + (9 - g.RA % 8) % 8) * EL;
     g.PSTR = (N * N + (9 - (N * N) % 8) % 8) * EL;
   }
-  size_t o = 128;  // 2*MAX_ST + 2 mbarriers (+ pad)
+  size_t o = 128;  // 2*MAX_ST + 2 mbarriers, MAX_ST fill counts (+ pad)
   g.BSTG = g.RA * g.BROW;
   g.FSTG = SG * g.FLS;
   if (TMA) {
@@ -311,15 +315,20 @@ __device__ __forceinline__ unsigned long long gtimer_ns() {
   asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
   return t;
 }
-// Wait for the phase with this parity, for at most WAIT_LIMIT_NS.  A thread
-// that already timed out does not wait again (its data are discarded at the
-// next block barrier).
-__device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, bool &to) {
+// Wait for the phase with this parity, for at most limit_ns (0: every wait
+// runs out at once, without polling).  A thread that already timed out does
+// not wait again (its data are discarded at the next block barrier).
+__device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, bool &to,
+                                          unsigned long long limit_ns) {
   if (to) return;
+  if (limit_ns == 0) {
+    to = true;
+    return;
+  }
   if (mbar_try_wait(bar, parity)) return;
   const unsigned long long t0 = gtimer_ns();
   while (!mbar_try_wait(bar, parity)) {
-    if (gtimer_ns() - t0 > WAIT_LIMIT_NS) {
+    if (gtimer_ns() - t0 >= limit_ns) {
       to = true;
       return;
     }
@@ -678,7 +687,8 @@ __global__ void __launch_bounds__(MAXT, MINB)
     calq32_kernel(int N, int S, int K2T, int NST, int NPL, int C, int GB,
                   const float *__restrict__ B32, const float2 *__restrict__ fin,
                   float2 *__restrict__ Q, float4 *__restrict__ partial, int tmap,
-                  const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmF) {
+                  unsigned long long wait_ns, const __grid_constant__ CUtensorMap tmB,
+                  const __grid_constant__ CUtensorMap tmF) {
   constexpr int SG = SC * WS;  // solves per group
   extern __shared__ __align__(128) unsigned char smem[];
   const C32Geom g =
@@ -687,6 +697,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);  // [MAX_ST]
   uint64_t *empty = full + MAX_ST;                       // [MAX_ST]
   uint64_t *pbar = full + 2 * MAX_ST;                    // [2] planes
+  int *fills = reinterpret_cast<int *>(pbar + 2);        // [MAX_ST] copies issued per stage
   float *Bs = reinterpret_cast<float *>(smem + g.off_B);
   float2 *fls = reinterpret_cast<float2 *>(smem + g.off_fl);
   float2 *plb = reinterpret_cast<float2 *>(smem + g.off_pl);
@@ -750,6 +761,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
     }
     mbar_init(&pbar[0], 1);
     mbar_init(&pbar[1], 1);
+    for (int i = 0; i < MAX_ST; ++i) fills[i] = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -776,11 +788,12 @@ __global__ void __launch_bounds__(MAXT, MINB)
   // Pipeline bookkeeping uses chunk-relative indices: j (line), pr (plane).
   // prologue: lines 0 .. NST-2 and the first plane
   int planes = 0;       // counted in warp 0
-  int jstop = nlines;   // first line not finished by every warp (abort drain)
   if (TMA && warp == 0 && nlines > 0) {
-    for (int j = 0; j < NST - 1 && j < nlines; ++j)
+    for (int j = 0; j < NST - 1 && j < nlines; ++j) {
       stage_line<true>(g, line_li(j), P0 * N + j, j % NST, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls,
                        full, tmap, &tmB, &tmF);
+      if (lane == 0) ++fills[j % NST];
+    }
     stage_plane<true>(g, (k1 - plane_l1(P0) + N) % N, u0, nval, NQ, fin, plb, &pbar[0]);
     ++planes;
   }
@@ -796,7 +809,6 @@ __global__ void __launch_bounds__(MAXT, MINB)
       // every warp is done with the previous plane (and with its buffer)
       if (__syncthreads_or(to)) {
         aborted = true;
-        jstop = j;
         break;
       }
       if (TMA) {
@@ -806,13 +818,13 @@ __global__ void __launch_bounds__(MAXT, MINB)
                               plb + (size_t)((pr + 1) & 1) * plane_sz, &pbar[(pr + 1) & 1]);
             ++planes;
           }
-          mbar_wait(&pbar[pr & 1], (uint32_t)((pr >> 1) & 1), to);
+          mbar_wait(&pbar[pr & 1], (uint32_t)((pr >> 1) & 1), to, wait_ns);
         } else {
           if (warp == 0 && pr > 0) {
             stage_plane<true>(g, (k1 - l1 + N) % N, u0, nval, NQ, fin, plb, &pbar[0]);
             ++planes;
           }
-          mbar_wait(&pbar[0], (uint32_t)(pr & 1), to);
+          mbar_wait(&pbar[0], (uint32_t)(pr & 1), to, wait_ns);
         }
       } else {
         stage_plane<false>(g, (k1 - l1 + N) % N, u0, nval, NQ, fin, plb, pbar);
@@ -822,15 +834,19 @@ __global__ void __launch_bounds__(MAXT, MINB)
       // refill: line j+NST-1 goes into the stage line j-1 used.  The issuing
       // warp rotates over the full warps with the line, so the issue work
       // (and the wait for every warp to leave line j-1) does not make one warp
-      // fall behind the rest.
+      // fall behind the rest.  Once one of its lanes has timed out the warp
+      // issues nothing more: the stage's previous copy may still be landing.
       const int jn = j + NST - 1;
       if (warp == jn % nfull && jn < nlines) {
         const int sn = jn % NST;
-        if (j >= 1) mbar_wait(&empty[sn], (uint32_t)(((j - 1) / NST) & 1), to);
-        stage_line<true>(g, line_li(jn), P0 * N + jn, sn, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full,
-                         tmap, &tmB, &tmF);
+        if (j >= 1) mbar_wait(&empty[sn], (uint32_t)(((j - 1) / NST) & 1), to, wait_ns);
+        if (!__any_sync(warp_mask(), to)) {
+          stage_line<true>(g, line_li(jn), P0 * N + jn, sn, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs,
+                           fls, full, tmap, &tmB, &tmF);
+          if (lane == 0) ++fills[sn];
+        }
       }
-      mbar_wait(&full[st], (uint32_t)((j / NST) & 1), to);
+      mbar_wait(&full[st], (uint32_t)((j / NST) & 1), to, wait_ns);
     } else {
       __syncthreads();  // previous line's readers are done (single buffer)
       stage_line<false>(g, li, P0 * N + j, st, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full,
@@ -857,8 +873,11 @@ __global__ void __launch_bounds__(MAXT, MINB)
         compute_line<false, false, A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
     }
     if (TMA) {
-      __syncwarp(warp_mask());
-      if (lane == 0) mbar_arrive(&empty[st]);
+      // a warp releases the stage only when every lane saw this line's copy
+      // land, so a stage is refilled only after its previous copy completed
+      // (at most one copy per stage is ever in flight)
+      const bool bad = __any_sync(warp_mask(), to);
+      if (lane == 0 && !bad) mbar_arrive(&empty[st]);
     }
     if ((l2 + 1) % FOLD_LINES == 0 || l2 == N - 1) {  // fold into the compensated pair
 #pragma unroll
@@ -893,18 +912,15 @@ __global__ void __launch_bounds__(MAXT, MINB)
   if (aborted) {
     if (tid == 0) {
       atomicExch(&g_calq32_status, 1);
-      // drain: wait for the last phase issued on every barrier, so no copy
-      // lands after the block exits
-      bool t2 = false;
+      // drain: wait for the last copy issued into every stage and plane
+      // buffer, so none lands after the block exits.  Fill k of a stage
+      // completes phase k of its full barrier, and a stage is refilled only
+      // after its previous fill landed, so only the last fill can be pending.
       if (TMA) {
-        // every warp finished iterations 0 .. jstop-1, each of which issued
-        // line i + NST - 1 after the NST - 1 lines of the prologue
-        const int issued = min(nlines, jstop + NST - 1);
         for (int sx = 0; sx < NST; ++sx) {
-          int last = -1;  // last line issued into stage sx
-          for (int x = issued - 1; x >= 0 && x >= issued - NST; --x)
-            if (x % NST == sx) last = x;
-          if (last >= 0) mbar_wait(&full[sx], (uint32_t)((last / NST) & 1), t2);
+          bool t2 = false;
+          if (fills[sx] > 0)
+            mbar_wait(&full[sx], (uint32_t)((fills[sx] - 1) & 1), t2, DRAIN_LIMIT_NS);
         }
         // plane x went to buffer (NPL == 2 ? x & 1 : 0); the last one issued into
         // each buffer is the only phase that can still be pending there
@@ -912,7 +928,8 @@ __global__ void __launch_bounds__(MAXT, MINB)
           if (px < 0) continue;
           const int b = (NPL == 2) ? (px & 1) : 0;
           const int use = (NPL == 2) ? (px >> 1) : px;
-          mbar_wait(&pbar[b], (uint32_t)(use & 1), t2);
+          bool t2 = false;
+          mbar_wait(&pbar[b], (uint32_t)(use & 1), t2, DRAIN_LIMIT_NS);
         }
       }
     }
@@ -1050,7 +1067,7 @@ static edb_status launch_c32(dim3 grid, int threads, size_t smem, int N, int S, 
   if (configured != cudaSuccess) return cuda_fail(configured, "cudaFuncSetAttribute(calq32)");
   calq32_kernel<TMA, MAXT, HLS, WS, A, MINB, PAIR>
       <<<grid, threads, smem, st>>>(N, S, K2T, NST, NPL, C, GB, B32, fin, Q, partial, maps.tmap,
-                                    maps.B, maps.F);
+                                    wait_limit_ns(), maps.B, maps.F);
   EDB_LAUNCHED();
   return EDB_OK;
 }
@@ -1151,7 +1168,7 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   if (GB > (int)grid.x) GB = (int)grid.x;
   if (vr.pair) {
     const long long n = (long long)((S + 1) / 2) * N * N * N;
-    const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+    const long long blocks = std::min<long long>((n + 255) / 256, 16LL * device_sm_count());
     c32_pairs_kernel<<<(unsigned)blocks, 256, 0, st>>>(S, (long long)N * N * N, d_fin, d_pairs);
     EDB_LAUNCHED();
   }
@@ -1162,7 +1179,7 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
                                       d_B32, src, d_Q, d_partial, maps, st);
   if (rc != EDB_OK || C == 1) return rc;
   const long long n = (long long)S * N * N * N;
-  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+  const long long blocks = std::min<long long>((n + 255) / 256, 16LL * device_sm_count());
   calq32_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(n, C, d_partial, d_Q);
   EDB_LAUNCHED();
   return EDB_OK;

@@ -105,7 +105,9 @@ __device__ __forceinline__ void df_axpy(DF2 &acc, u64 sh2, u64 nsh2, u64 nsl2, u
 }
 
 constexpr int DEPTH = 8;  // B rows in flight per warp
-constexpr unsigned long long WAIT_LIMIT_NS = 200000000ull;
+// Limit of the drain after a wait ran out: lane 0 then waits this long at
+// most for each copy its warp issued, so none lands after the block exits.
+constexpr unsigned long long DRAIN_LIMIT_NS = 1000000000ull;
 
 __device__ __forceinline__ uint32_t s_addr(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -142,12 +144,20 @@ __device__ __forceinline__ unsigned long long gtimer_ns() {
   asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
   return t;
 }
-__device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, bool &to) {
+// Wait for the phase with this parity, for at most limit_ns (0: every wait
+// runs out at once, without polling); a thread that timed out does not wait
+// again.
+__device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, bool &to,
+                                          unsigned long long limit_ns) {
   if (to) return;
+  if (limit_ns == 0) {
+    to = true;
+    return;
+  }
   if (mbar_try_wait(bar, parity)) return;
   const unsigned long long t0 = gtimer_ns();
   while (!mbar_try_wait(bar, parity)) {
-    if (gtimer_ns() - t0 > WAIT_LIMIT_NS) {
+    if (gtimer_ns() - t0 >= limit_ns) {
       to = true;
       return;
     }
@@ -203,13 +213,15 @@ __global__ void b2_pair_split_kernel(int N, const double *__restrict__ B, float2
 template <bool TMA, int MINB>
 __global__ void __launch_bounds__(256, MINB)
     calq64x_kernel(QParams p, int J2T, int LC, int paired, const float2 *__restrict__ B2,
-                   const float4 *__restrict__ fdf, double2 *__restrict__ partial) {
+                   const float4 *__restrict__ fdf, double2 *__restrict__ partial,
+                   unsigned long long wait_ns) {
   extern __shared__ __align__(128) unsigned char smem64[];
   const int N = p.N, P = p.P;
   const int R4 = (P + RUN - 1) / RUN;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nwarps = (blockDim.x + 31) >> 5;
   const int wthreads = min(32, (int)blockDim.x - warp * 32);  // threads in this warp
+  const unsigned wmask = wthreads == 32 ? 0xffffffffu : ((1u << wthreads) - 1u);
   const long long NN = (long long)N * N;
   // shared memory: [nwarps][DEPTH] mbarriers, B rings [nwarps][DEPTH][32 threads x 4 pairs],
   // then the f-hat plane [N][N]
@@ -260,6 +272,7 @@ __global__ void __launch_bounds__(256, MINB)
   const uint32_t seg_bytes = (uint32_t)(wthreads * RUN * sizeof(float2));
   const int nrows = (c1 - c0) * N;  // rows this CTA streams
   bool to = false;
+  int issued = 0;  // lane 0: rows its warp has issued into the ring
   // refill cursor (lane 0): row q + DEPTH of the chunk as (list plane, i2, i3),
   // advanced by one row per refill so the per-row path has no division
   int rf_pi = 0, rf_i2 = 0, rf_i3 = 0;
@@ -277,12 +290,13 @@ __global__ void __launch_bounds__(256, MINB)
       for (int d = 0; d < DEPTH; ++d) mbar_init(&mybar[d], 1);
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    __syncwarp();
+    __syncwarp(wmask);
     if (lane == 0) {  // prologue: the first DEPTH rows
       for (int q = 0; q < DEPTH && q < nrows; ++q) {
         const long long lflat = row_of(q);
         mbar_expect_tx(&mybar[q], seg_bytes);
         bulk_g2s(myring + (size_t)q * 32 * RUN, B2 + lflat * p.KC + wcol, seg_bytes, &mybar[q]);
+        ++issued;
       }
     }
   }
@@ -341,7 +355,7 @@ __global__ void __launch_bounds__(256, MINB)
         if (i3 >= N) break;
         if (TMA) {
           const int slot = q % DEPTH;
-          mbar_wait(&mybar[slot], (uint32_t)((q / DEPTH) & 1), to);
+          mbar_wait(&mybar[slot], (uint32_t)((q / DEPTH) & 1), to, wait_ns);
           const float4 *src = reinterpret_cast<const float4 *>(myring + ((size_t)slot * 32 + lane) * RUN);
 #pragma unroll
           for (int h = 0; h < RUN / 2; ++h) {
@@ -349,8 +363,11 @@ __global__ void __launch_bounds__(256, MINB)
             bcur[2 * h] = make_float2(v.x, v.y);
             bcur[2 * h + 1] = make_float2(v.z, v.w);
           }
-          __syncwarp();
-          if (lane == 0 && q + DEPTH < nrows) {  // refill this slot with row q + DEPTH
+          // every lane has read the slot; refill it with row q + DEPTH unless a
+          // lane timed out (its copy may still be landing: the warp then
+          // issues nothing more, so at most one copy per slot is in flight)
+          const bool bad = __any_sync(wmask, to);
+          if (lane == 0 && !bad && q + DEPTH < nrows) {
             const long long lflat = rf_base + rf_i3;
             if (++rf_i3 == N) {
               rf_i3 = 0;
@@ -364,6 +381,7 @@ __global__ void __launch_bounds__(256, MINB)
             mbar_expect_tx(&mybar[slot], seg_bytes);
             bulk_g2s(myring + (size_t)slot * 32 * RUN, B2 + lflat * p.KC + wcol, seg_bytes,
                      &mybar[slot]);
+            ++issued;
           }
         } else if (i3 + 1 < N) {
           const float2 *bn = brow + (long long)(i3 + 1) * p.KC;
@@ -409,11 +427,16 @@ __global__ void __launch_bounds__(256, MINB)
     if (__syncthreads_or(to)) {
       if (lane == 0) {
         atomicExch(&g_calq64x_status, 1);
-        bool t2 = false;  // drain the slots still in flight
-        for (int qq = (nrows > DEPTH ? nrows - DEPTH : 0); qq < nrows; ++qq)
-          mbar_wait(&mybar[qq % DEPTH], (uint32_t)((qq / DEPTH) & 1), t2);
+        // drain: row r went into slot r % DEPTH as its fill r / DEPTH, and a
+        // slot is refilled only after its previous copy landed, so only the
+        // last row issued into each slot can still be in flight
+        for (int sl = 0; sl < DEPTH && sl < issued; ++sl) {
+          const int last = sl + ((issued - 1 - sl) / DEPTH) * DEPTH;
+          bool t2 = false;
+          mbar_wait(&mybar[sl], (uint32_t)((last / DEPTH) & 1), t2, DRAIN_LIMIT_NS);
+        }
       }
-      __syncwarp();
+      __syncwarp(wmask);
       return;
     }
   }
@@ -492,9 +515,7 @@ static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int minb, bool
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, pl.threads, pl.smem);
   if (occ < 1) occ = 1;
-  int sms = 152, dev = 0;
-  if (cudaGetDevice(&dev) == cudaSuccess)
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = device_sm_count();
   const long long wave = (long long)sms * occ;
   const long long per_chunk = (long long)p.P * tiles;
   const int NL = c64x_lines(p, paired);
@@ -564,20 +585,31 @@ edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const float4 *d_
   if (pl.tma) {
     if (minb == 2)
       calq64x_kernel<true, 2><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf,
-                                                                 d_partial);
+                                                                 d_partial, wait_limit_ns());
     else
       calq64x_kernel<true, 1><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf,
-                                                                 d_partial);
+                                                                 d_partial, wait_limit_ns());
   } else {
     if (minb == 2)
       calq64x_kernel<false, 2><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf,
-                                                                  d_partial);
+                                                                  d_partial, wait_limit_ns());
     else
       calq64x_kernel<false, 1><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf,
-                                                                  d_partial);
+                                                                  d_partial, wait_limit_ns());
   }
   EDB_LAUNCHED();
   return launch_calq64_reduce(p, pl.nch, d_partial, d_Q, st);
+}
+
+edb_status read_calq64x_status(int *status, bool clear) {
+  int v = 0;
+  EDB_CUDA(cudaMemcpyFromSymbol(&v, g_calq64x_status, sizeof(int)));
+  if (clear && v) {
+    int z = 0;
+    EDB_CUDA(cudaMemcpyToSymbol(g_calq64x_status, &z, sizeof(int)));
+  }
+  *status = v;
+  return EDB_OK;
 }
 
 }  // namespace edb

@@ -34,8 +34,8 @@ __device__ __forceinline__ double flogf_dev(double f) {
   return f * log(f) - f;
 }
 
-// sum over f_i > eps of f_i log f_i (EntropyFix.h:194-199) of
-// fMid_i = beta*avg + (1-beta) f_i (FixSol's trial state, :282-287), or of
+// sum over f_i > eps of f_i log f_i (EntropyFix.h:139-143) of
+// fMid_i = beta*avg + (1-beta) f_i (FixSol's trial state, :226-231), or of
 // f_i itself when beta_bar < 0.
 __device__ double efix_sum(const double2 *F, const double *f, long long Nf, double betaFbar,
                            double omb, bool trial, double eps, double *red) {
@@ -66,7 +66,7 @@ struct AvgSnap {
   int flag;
 };
 
-// FixSol (EntropyFix.h:268-309) on Re F (F != null, imaginary parts zeroed as
+// FixSol (EntropyFix.h:211-253) on Re F (F != null, imaginary parts zeroed as
 // BKW.h:232 does) or on a real array f.  `snap` lives in shared memory and is
 // block-uniform on entry and exit.  The bisection halves [betaL, betaR] until
 // its width is <= eps (about 34 halvings from [0,1] at eps = 1e-10), so the
@@ -383,7 +383,8 @@ __global__ void c2r_kernel(long long n, const double2 *__restrict__ y, double *_
 }
 
 edb_status launch_complex_to_real(long long n, const double2 *y, double *x, cudaStream_t st) {
-  const long long blocks = (n + 255) / 256 < 152LL * 32 ? (n + 255) / 256 : 152LL * 32;
+  const long long cap = 32LL * device_sm_count();
+  const long long blocks = (n + 255) / 256 < cap ? (n + 255) / 256 : cap;
   c2r_kernel<<<(unsigned)blocks, 256, 0, st>>>(n, y, x);
   EDB_LAUNCHED();
   return EDB_OK;

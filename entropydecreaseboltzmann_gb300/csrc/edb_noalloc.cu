@@ -12,13 +12,16 @@
 //
 // The array's name, used in host code, is only a host-side stand-in for the
 // device symbol and is never handed to a kernel.  Its device address is
-// looked up with cudaGetSymbolAddress once per device, with that device
-// current, on the entry point's first call there; that first call should
-// therefore come before any stream capture.  Every call on a device reuses
+// looked up with cudaGetSymbolAddress once per device context, with that
+// device current, on the entry point's first call there (and again after the
+// device's primary context was reset, which reloads the module at another
+// address); that first call should therefore come before any stream capture.  Every call on a device reuses
 // the same array, so calls that overlap on the GPU (two streams, or two host
 // threads) race on it; serialise them.  The array keeps the previous call's
 // contents; nothing needs clearing, because every partial sum is written
 // before it is read.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "edb_internal.cuh"
@@ -34,6 +37,23 @@ static __device__ __align__(256) double2 g_noalloc_scratch[kNoallocScratchEntrie
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 double2 *g_scratch_addr[kMaxDevices] = {};
+CUcontext g_scratch_ctx[kMaxDevices] = {};  // context the address belongs to
+
+// cuCtxGetCurrent from the driver, through the runtime's entry-point query
+// (the library links no driver stub).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+CtxGetCurrentFn ctx_get_current() {
+  static const CtxGetCurrentFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(p);
+  }();
+  return fn;
+}
 
 }  // namespace
 
@@ -53,14 +73,23 @@ extern "C" edb_status edb_calQ_fp64_noalloc(int N, int index_mode, const double 
   int dev = 0;
   EDB_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(EDB_EINVAL, "device ordinal out of range");
+  // the runtime makes the device's primary context current on its first call;
+  // cudaFree(0) would too, but this entry point must not call it
+  CUcontext ctx = nullptr;
+  const CtxGetCurrentFn get_ctx = ctx_get_current();
+  if (!get_ctx) return fail(EDB_ECUDA, "noalloc calQ: cuCtxGetCurrent is not available");
   double2 *scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
+    if (get_ctx(&ctx) != CUDA_SUCCESS) ctx = nullptr;
+    if (!g_scratch_addr[dev] || !ctx || ctx != g_scratch_ctx[dev]) {
       void *addr = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
       if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
       g_scratch_addr[dev] = static_cast<double2 *>(addr);
+      // the symbol lookup has made the primary context current
+      if (get_ctx(&ctx) != CUDA_SUCCESS) ctx = nullptr;
+      g_scratch_ctx[dev] = ctx;
     }
     scratch = g_scratch_addr[dev];
   }

@@ -167,10 +167,13 @@ int edb_qcalc_batch_variants(void);
  * cudaMalloc's implicit synchronisation).  No counterpart in the reference.
  * The caller passes the FP64 table d_B (N^3 x N^3 doubles, the layout genB
  * produces; see edb_qcalc_copy_B), d_fin and d_Qout (N^3 complex doubles each,
- * FFTW order); the result equals edb_qcalc_calQ_device's.  The partial sums
- * live in one fixed 5 MiB device array per device, which every GPU that loads
- * the library holds until exit; N must be in [3, 64].  The first call on a
- * device looks up that array's address, so make it before any stream capture.
+ * FFTW order); the result agrees with edb_qcalc_calQ_device's to 1e-12
+ * relative L2 (it runs the native-FP64 kernel on the full table, the handle
+ * path by default the double-float kernel, in another summation order).  The
+ * partial sums live in one fixed 5 MiB device array per device, which every
+ * GPU that loads the library holds until exit; N must be in [3, 64].  The
+ * first call on a device (and the first after its primary context was reset)
+ * looks up that array's address, so make it before any stream capture.
  * Calls that overlap on the GPU share the array and race: serialise them. */
 edb_status edb_calQ_fp64_noalloc(int N, int index_mode, const double *d_B, const double *d_fin,
                                  double *d_Qout, void *stream);
@@ -182,10 +185,24 @@ edb_status edb_calQ_fp64_noalloc(int N, int index_mode, const double *d_B, const
 edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float *d_fin, float *d_Qout,
                                     void *stream, int *chosen);
 
-/* Device status word of the batched kernel: nonzero when one of its bounded
- * waits ran out (the launch then returned early and its output is invalid).
- * clear != 0 resets it.  No reference counterpart. */
+/* Device status words of the Q-hat kernels (no reference counterpart): bit 0
+ * set when a bounded wait inside the batched kernel ran out, bit 1 when one
+ * inside the double-float FP64 kernel did (that launch then returned early,
+ * after its copies in flight had landed, and its output is invalid).
+ * clear != 0 resets them.  The synchronous entry points (edb_qcalc_calQ,
+ * edb_qcalc_genB, edb_solver_run, edb_batch_step with a NULL stream) read
+ * and clear them themselves and return EDB_ETIMEDOUT; after stream-ordered
+ * calls, read them here. */
 edb_status edb_device_status(int *status, int clear);
+
+/* Limit of each bounded wait inside the Q-hat kernels (no reference
+ * counterpart), in nanoseconds: ns < 0 restores the default of 200 ms, and
+ * 0 makes every wait run out at once, without polling.  It is
+ * read at each launch (graphs captured earlier keep the limit they were
+ * captured with).  For tests of the timeout path: a wait that runs out makes
+ * the kernel drain the copies it issued and return, and the entry point
+ * report EDB_ETIMEDOUT. */
+edb_status edb_set_wait_limit_ns(long long ns);
 
 /* Kernel of the FP64 collision sum (edb_qcalc_calQ, _device, the integrator).
  * EMULATED (default): FP64-accurate double-float arithmetic on the FP32 pipe,

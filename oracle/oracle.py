@@ -23,6 +23,19 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libedb_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libedbref.so")
+# Where the reference's sources are read from: the EDB_REFERENCE_DIR
+# environment variable (the reference repository's root), by default the
+# read-only copy this build was made against.  Only the build of the compiled
+# reference (`make ref`) and the tests that compile the reference's drivers
+# read it; nothing on a GPU host does.
+REF_ROOT = os.environ.get("EDB_REFERENCE_DIR", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "CalQ")
+
+
+def reference_sources_present() -> bool:
+    """True where the reference's CalQ sources can be read."""
+    return os.path.isfile(os.path.join(REF_SRC, "QCalculator.h"))
+
 
 INDEX_REFERENCE = 0
 INDEX_ALIASED = 1
@@ -41,7 +54,7 @@ def _ptr(a: np.ndarray):
 def build_oracle(ref: bool = False) -> None:
     """Compile the restatement (and, if ``ref``, the reference) with make."""
     targets = ["all"] + (["ref"] if ref else [])
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+    subprocess.run(["make", "-s", "-C", HERE, f"REF_SRC={REF_SRC}"] + targets, check=True)
 
 
 class Oracle:
@@ -324,6 +337,30 @@ class Reference:
                                    buf, log_cap)
         assert rc == 0
         return Fhat, F, buf.value.decode()
+
+    def run_from(self, N, R, scheme, F0, T0, TEnd, dt, checks):
+        """RK4 or SSP3 step sequence of the reference's objects from the given
+        real-space initial data (edbref_run_from).  Returns (Fhat, F) at the
+        1-based steps in ``checks`` (arrays of shape [len(checks), N^3]) and the
+        per-step entropy before / after the fix rule."""
+        nq = N ** 3
+        F0 = np.ascontiguousarray(F0, dtype=np.complex128).reshape(-1)
+        chk = np.ascontiguousarray(checks, dtype=np.int32)
+        Fh = np.empty((chk.size, nq), dtype=np.complex128)
+        F = np.empty((chk.size, nq), dtype=np.complex128)
+        cap = int(chk.max()) + 16
+        raw = np.empty(cap)
+        fixed = np.empty(cap)
+        sch = SCHEMES[scheme] if isinstance(scheme, str) else int(scheme)
+        fn = self.L.edbref_run_from
+        fn.restype = C.c_int
+        fn.argtypes = [C.c_int, C.c_double, C.c_int, _dp, C.c_double, C.c_double, C.c_double,
+                       C.c_int, _ip, _dp, _dp, _dp, _dp, C.c_int]
+        n = fn(N, float(R), sch, _ptr(F0.view(np.float64)), float(T0), float(TEnd), float(dt),
+               chk.size, chk.ctypes.data_as(_ip), _ptr(Fh.view(np.float64)),
+               _ptr(F.view(np.float64)), _ptr(raw), _ptr(fixed), cap)
+        assert n >= int(chk.max()), n
+        return Fh, F, raw[:n].copy(), fixed[:n].copy()
 
 
 class RefQCalculator:

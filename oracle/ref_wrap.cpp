@@ -190,6 +190,83 @@ int edbref_bkw_fe_files(int N, double R, double T0, double TEnd, double dt, int 
   return 0;
 }
 
+// The step sequence of BKW3D::RK4 (BKW.h:452-519) or BKW3D::SSP3 (:387-449)
+// from caller-given real-space initial data F0 (N^3 interleaved complex).
+// The reference's integrators always start from setInitialValue's live
+// funExact branch (BKW.h:96-110, a sinusoid), so a run from other data (the
+// BKW profile, a Maxwellian mixture) drives the reference's own objects here:
+// BKW3D's F / Fhat arrays, fft3 and calEntropy, QCalculator(N0, 0) with genB
+// and calQ, EntropyFix::FixSol.  Only the loop is spelled out, with the stage
+// expressions written exactly as BKW.h:416-424 and :483-494 write them (same
+// operand order, so the same rounding).  scheme: 3 SSP3, 4 RK4.  After each
+// step listed in check_steps (1-based, increasing) Fhat and F are copied into
+// row c of Fhat_out / F_out; ent_raw / ent_fixed receive every step's entropy
+// before and after the fix rule (cap entries).  Returns the number of steps.
+int edbref_run_from(int N, double R, int scheme, const double *F0, double T0, double TEnd,
+                    double dt, int ncheck, const int *check_steps, double *Fhat_out,
+                    double *F_out, double *ent_raw, double *ent_fixed, int cap) {
+  if (scheme != 3 && scheme != 4) return -1;
+  CoutCapture cap_out;
+  BK b(N, R);
+  const int N3d = b.N3d;
+  std::memcpy((double *)b.F, F0, sizeof(double) * 2 * N3d);
+  b.fft3();  // BKW.h:198 (forward)
+  QC qcal(N, 0);
+  qcal.genB();
+  EF efix(N3d);
+  std::vector<c_t> F1(N3d), F2(N3d), F3(N3d), Q1(N3d), Q2(N3d), Q3(N3d);
+  std::vector<double> Ftmp(N3d);
+  c_t *Fhat = b.Fhat, *Q = b.Q, *F = b.F;
+  double t = T0, entropy, entropy0 = 1.;
+  int step = 0, c = 0, done = 0;
+  do {
+    t += dt;
+    if (scheme == 4) {  // BKW.h:482-494
+      qcal.calQ(Q, Fhat);
+      for (int l = 0; l < N3d; ++l) F1[l] = Fhat[l] + 0.5 * dt * Q[l];
+      qcal.calQ(Q1.data(), F1.data());
+      for (int l = 0; l < N3d; ++l) F2[l] = Fhat[l] + 0.5 * dt * Q1[l];
+      qcal.calQ(Q2.data(), F2.data());
+      for (int l = 0; l < N3d; ++l) F3[l] = Fhat[l] + dt * Q2[l];
+      qcal.calQ(Q3.data(), F3.data());
+      for (int l = 0; l < N3d; ++l)
+        Fhat[l] = Fhat[l] + dt / 6. * (Q[l] + 2. * Q1[l] + 2. * Q2[l] + Q3[l]);
+    } else {  // BKW.h:416-424
+      qcal.calQ(Q, Fhat);
+      for (int l = 0; l < N3d; ++l) F1[l] = Fhat[l] + dt * Q[l];
+      qcal.calQ(Q, F1.data());
+      for (int l = 0; l < N3d; ++l) F2[l] = 0.75 * Fhat[l] + 0.25 * F1[l] + 0.25 * dt * Q[l];
+      qcal.calQ(Q, F2.data());
+      for (int l = 0; l < N3d; ++l)
+        Fhat[l] = Fhat[l] / 3. + 2. * F2[l] / 3. + 2. / 3. * dt * Q[l];
+    }
+    b.fft3(true);  // BKW.h:428 / :498
+    entropy = b.calEntropy();
+    const double raw = entropy;
+    if (step) {  // the fix rule of BKW.h:431-440 / :501-510
+      if (entropy - entropy0 > 1.0e-10) {
+        for (int i = 0; i < N3d; ++i) Ftmp[i] = std::real(F[i]);
+        efix.FixSol(N * N * N, Ftmp.data(), entropy0 / (std::pow(2 * R, 3)));
+        for (int i = 0; i < N3d; ++i) F[i] = c_t{Ftmp[i]};
+        entropy = b.calEntropy();
+      }
+    }
+    if (done < cap) {
+      ent_raw[done] = raw;
+      ent_fixed[done] = entropy;
+    }
+    entropy0 = entropy;
+    step++;
+    done++;
+    if (c < ncheck && done == check_steps[c]) {
+      std::memcpy(Fhat_out + (size_t)c * 2 * N3d, (double *)Fhat, sizeof(double) * 2 * N3d);
+      std::memcpy(F_out + (size_t)c * 2 * N3d, (double *)F, sizeof(double) * 2 * N3d);
+      ++c;
+    }
+  } while (t < TEnd);
+  return done;
+}
+
 // Times the reference calQ: `reps` calls on the same input; returns seconds
 // per call (steady_clock).  Used only as a CPU baseline where the reference
 // sources exist.

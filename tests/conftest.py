@@ -34,7 +34,9 @@ def reference():
     from oracle.oracle import REF_SO, Reference, build_oracle
 
     if not os.path.exists(REF_SO):
-        if not os.path.isdir("/root/reference/CalQ"):
+        from oracle.oracle import reference_sources_present
+
+        if not reference_sources_present():
             pytest.skip("reference sources not present on this host")
         build_oracle(ref=True)
     return Reference()

@@ -20,6 +20,26 @@ own CalQ headers and records, for fixed seeds:
 
 The FFTs inside those runs come from the in-repo FFTW-API shim, because FFTW
 is not installed here; its conventions are FFTW's documented ones.
+
+A second file, tests/golden/reference_golden_configs.npz, holds the cases at
+the workloads' sizes (``--configs`` regenerates only it):
+
+* the testBKW3D case on RK4 (CalQ/BKW.h:452-519): N = 16 on [-6, 6]^3,
+  dt = 0.01, 100 steps, the reference's QCalculator(N0, 0).  Once from the
+  BKW profile at t0 = 5.5 (K = 1 - exp(-t0/6), CalQ/testfft.cpp:11-16):
+  Fhat after steps 1, 10, 50 and 100, F after step 100, and every step's
+  entropy before / after the fix rule.  Once more from the reference's own
+  initial data (setInitialValue's live sinusoid branch, BKW.h:96-138) for
+  10 steps (after step 10 that run turns most modes into NaN under the
+  even-N loops); it is checked here to be bit-identical to the reference's
+  own BKW3D::RK4;
+* SSP3 with the fix rule (BKW.h:387-449), 10 steps of dt = 0.005, on
+  [-6.62132, 6.62132]^3: N = 16 from the sinusoid (the fix acts on steps
+  2-10) and N = 15, 17 from a seeded two-Maxwellian mixture;
+* QCalculator::calQ at N = 24 (Maxwell, filter on) and N = 25 (hard sphere,
+  filter off) on integer-valued inputs.
+Runs from data other than the sinusoid go through oracle/ref_wrap.cpp's
+edbref_run_from, which drives the reference's own objects.
 """
 import os
 import sys
@@ -33,6 +53,67 @@ sys.path.insert(0, ROOT)
 from oracle.oracle import Reference, build_oracle, _ptr  # noqa: E402
 
 R = 6.62132
+
+
+def _data_module():
+    # the initial-data helpers, loaded by path (importing the package would
+    # load its CUDA library)
+    import importlib.util
+
+    path = os.path.join(ROOT, "entropydecreaseboltzmann_gb300", "data.py")
+    spec = importlib.util.spec_from_file_location("edb_data", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+CFG1_CHECKS = [1, 10, 50, 100]
+CFG1_SIN_CHECKS = [1, 5, 10]
+
+
+def configs(ref):
+    data = _data_module()
+    out = {}
+    # ---- the testBKW3D case on RK4: N = 16, R = 6, dt = 0.01, 100 steps
+    N, Rb, dt = 16, 6.0, 0.01
+    # the sinusoid under the even-N loops turns most modes into NaN between
+    # steps 10 and 19, so that run stops at step 10
+    for tag, F0, checks in (("sin", ref.initial(N, Rb), CFG1_SIN_CHECKS),
+                            ("bkw", data.bkw_grid(N, Rb, 5.5), CFG1_CHECKS)):
+        TEnd = (checks[-1] - 0.5) * dt  # `do { t += dt } while (t < TEnd)`: checks[-1] steps
+        Fh, F, raw, fixed = ref.run_from(N, Rb, "RK4", F0, 0.0, TEnd, dt, checks)
+        assert np.all(np.isfinite(Fh)) and np.all(np.isfinite(F))
+        out[f"cfg1_{tag}_F0"] = np.asarray(F0, dtype=np.complex128)
+        out[f"cfg1_{tag}_Fhat"] = Fh
+        out[f"cfg1_{tag}_F"] = F[-1]
+        out[f"cfg1_{tag}_ent_raw"] = raw
+        out[f"cfg1_{tag}_ent_fixed"] = fixed
+        out[f"cfg1_{tag}_checks"] = np.array(checks)
+        if tag == "sin":  # the reference's own driver gives the same bits
+            Fl, Fll, _ = ref.run(N, Rb, "RK4", 0.0, TEnd, dt, fix=True)
+            assert np.array_equal(Fl, Fh[-1]) and np.array_equal(Fll, F[-1])
+    # ---- SSP3 with the fix rule, N = 15 / 16 / 17, 10 steps of dt = 0.005
+    dt3 = 0.005
+    for N in (15, 16, 17):
+        F0 = ref.initial(N, R) if N == 16 else data.two_maxwellians(N, R, 100 + N)
+        Fh, F, raw, fixed = ref.run_from(N, R, "SSP3", F0, 0.0, 9.5 * dt3, dt3, [10])
+        out[f"ssp3_N{N}_F0"] = np.asarray(F0, dtype=np.complex128)
+        out[f"ssp3_N{N}_Fhat"] = Fh[0]
+        out[f"ssp3_N{N}_F"] = F[0]
+        out[f"ssp3_N{N}_ent_raw"] = raw
+        out[f"ssp3_N{N}_ent_fixed"] = fixed
+    # ---- calQ at the workloads' N (REFERENCE loops; odd N = the aliased sum)
+    rng = np.random.default_rng(20211024)
+    for N, alpha, filt in ((24, 0, True), (25, 1, False)):
+        tag = f"N{N}_a{alpha}_f{int(filt)}"
+        q = ref.qcalc(N, alpha, filt)
+        fin = rng.integers(0, 10, N ** 3) + 1j * rng.integers(0, 10, N ** 3)
+        out[f"calq_in_{tag}"] = fin
+        out[f"calq_out_{tag}"] = q.calQ(fin)
+        del q
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_golden_configs.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes,", len(out), "arrays")
 
 
 def main():
@@ -129,4 +210,9 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if "--configs" in sys.argv:
+        build_oracle(ref=True)
+        configs(Reference())
+    else:
+        main()
+        configs(Reference())

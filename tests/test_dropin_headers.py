@@ -12,7 +12,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CPP = os.path.join(ROOT, "entropydecreaseboltzmann_gb300", "cpp")
 INC = os.path.join(ROOT, "include")
 PKG = os.path.join(ROOT, "entropydecreaseboltzmann_gb300")
-REF = "/root/reference/CalQ"
+from oracle.oracle import REF_SRC as REF  # noqa: E402
 
 
 def gxx():

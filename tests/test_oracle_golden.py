@@ -159,3 +159,54 @@ def test_reference_output_files_fixture(reference, tmp_path):
         os.chdir(cwd)
     for got, want in (("F.dat", "ref_FE_N6_F.dat"), ("slice.dat", "ref_FE_N6_slice.dat")):
         assert (tmp_path / got).read_bytes() == open(os.path.join(here, want), "rb").read()
+
+
+# ---- the workloads' sizes (tests/golden/reference_golden_configs.npz)
+
+@pytest.fixture(scope="module")
+def cfg():
+    import os
+
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_golden_configs.npz"))
+
+
+@pytest.mark.parametrize("tag", ["sin", "bkw"])
+def test_config1_rk4_oracle_matches_reference(oracle, cfg, tag):
+    """The testBKW3D case on RK4 (N = 16, [-6, 6]^3, dt = 0.01): the oracle's
+    restated step sequence from the same initial data gives the reference's
+    bits after 10 steps (the checkpoint both fixtures hold)."""
+    checks = list(cfg[f"cfg1_{tag}_checks"])
+    i = checks.index(10)
+    Fh, F, raw, fixed = oracle.run(16, 6.0, "RK4", 0.0, 9.5 * 0.01, 0.01, fix=True,
+                                   F0=cfg[f"cfg1_{tag}_F0"])
+    assert np.array_equal(Fh, cfg[f"cfg1_{tag}_Fhat"][i])
+    np.testing.assert_array_equal(raw, cfg[f"cfg1_{tag}_ent_raw"][:10])
+    np.testing.assert_array_equal(fixed, cfg[f"cfg1_{tag}_ent_fixed"][:10])
+    if tag == "sin":
+        assert np.array_equal(F, cfg["cfg1_sin_F"])
+
+
+@pytest.mark.parametrize("N", [15, 16, 17])
+def test_ssp3_fix_oracle_matches_reference(oracle, cfg, N):
+    """SSP3 with the fix rule, 10 steps of dt = 0.005 (the fix acts on steps
+    2-10 at N = 16): bit-identical final Fhat, F and entropy traces."""
+    Fh, F, raw, fixed = oracle.run(N, R_REFERENCE, "SSP3", 0.0, 9.5 * 0.005, 0.005, fix=True,
+                                   F0=cfg[f"ssp3_N{N}_F0"])
+    assert np.array_equal(Fh, cfg[f"ssp3_N{N}_Fhat"])
+    assert np.array_equal(F, cfg[f"ssp3_N{N}_F"])
+    np.testing.assert_array_equal(raw, cfg[f"ssp3_N{N}_ent_raw"])
+    np.testing.assert_array_equal(fixed, cfg[f"ssp3_N{N}_ent_fixed"])
+    if N == 16:
+        assert np.count_nonzero(raw != fixed) >= 5  # the fix acted
+
+
+def test_calQ_N25_direct_modes_match_reference(oracle, cfg):
+    """calQ at N = 25 (odd: the reference's loops are the aliased sum) against
+    the oracle's direct evaluation at 64 modes, relative L2 <= 1e-13 (the two
+    sums run in different orders)."""
+    N = 25
+    fin = cfg["calq_in_N25_a1_f0"]
+    want = cfg["calq_out_N25_a1_f0"]
+    k = np.random.default_rng(25).choice(N ** 3, 64, replace=False)
+    got = oracle.direct_modes(N, fin, k, gamma=1.0, R=R_REFERENCE, filter=False)
+    assert np.linalg.norm(got - want[k]) <= 1e-13 * np.linalg.norm(want[k])
