@@ -18,12 +18,13 @@ include/edb.h).  There is no CPU fallback.
 """
 from ._lib import (INDEX_ALIASED, INDEX_REFERENCE, R_REFERENCE, SCHEME_CFE, SCHEME_DUFORT,
                    SCHEME_FE, SCHEME_RK2, SCHEME_RK4, SCHEME_SSP3, EdbError, lib)
-from .api import (BKW3D, BatchSolver, EntropyFix, QCalculator, Server, device_status, fft3d,
+from .api import (BKW3D, BatchSolver, CellSolver, EntropyFix, QCalculator, Server,
+                  device_status, fft3d,
                   kernel_launch_count, maxwellian_fit, moments_hat, moments_project,
                   set_wait_limit_ns)
 
 __all__ = [
-    "QCalculator", "fft3d", "EntropyFix", "BKW3D", "BatchSolver", "EdbError",
+    "QCalculator", "fft3d", "EntropyFix", "BKW3D", "BatchSolver", "CellSolver", "EdbError",
     "INDEX_REFERENCE", "INDEX_ALIASED", "R_REFERENCE", "SCHEME_FE", "SCHEME_CFE", "SCHEME_RK2",
     "SCHEME_SSP3", "SCHEME_RK4", "SCHEME_DUFORT", "kernel_launch_count", "device_status", "lib",
     "moments_hat", "moments_project", "maxwellian_fit", "Server", "set_wait_limit_ns",

@@ -17,7 +17,8 @@ LIB_PATH = os.path.join(_HERE, "libedb.so")
 
 EDB_OK = 0
 STATUS = {0: "EDB_OK", 1: "EDB_EINVAL", 2: "EDB_ENOMEM", 3: "EDB_ECUDA", 4: "EDB_ETIMEDOUT",
-          5: "EDB_ENOTREADY", 6: "EDB_EBUSY", 7: "EDB_ENOTFOUND"}
+          5: "EDB_ENOTREADY", 6: "EDB_EBUSY", 7: "EDB_ENOTFOUND", 8: "EDB_ECANCELED",
+          9: "EDB_ENONFINITE"}
 INDEX_REFERENCE = 0
 INDEX_ALIASED = 1
 R_REFERENCE = 6.62132
@@ -77,7 +78,8 @@ class ServerStats(C.Structure):
                 ("qhat_evals", C.c_double), ("qhat_evals_padded", C.c_double),
                 ("qhat_evals_per_s", C.c_double), ("steps_launched", C.c_longlong),
                 ("kernel_launches", C.c_longlong), ("hbm_bytes_peak", C.c_double),
-                ("groups", C.c_int), ("refused", C.c_longlong)]
+                ("groups", C.c_int), ("refused", C.c_longlong), ("cancelled", C.c_longlong),
+                ("failed", C.c_longlong)]
 
 
 _dp = C.POINTER(C.c_double)
@@ -141,6 +143,9 @@ def _load():
         "edb_batch_load_device": (C.c_int, [_vp, _vp, _vp]),
         "edb_batch_step": (C.c_int, [_vp, C.c_int, _vp]),
         "edb_batch_read": (C.c_int, [_vp, _dp, _dp]),
+        "edb_batch_read_device": (C.c_int, [_vp, _vp, _vp]),
+        "edb_cells_transport_x_device": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double,
+                                                   C.c_double, _vp, _vp, _vp]),
         "edb_batch_moments": (C.c_int, [_vp, _dp, _dp]),
         "edb_batch_launches_per_step": (C.c_int, [_vp, _ip]),
         "edb_qcalc_genB_f32": (C.c_int, [_vp]),
@@ -154,6 +159,7 @@ def _load():
         "edb_server_start": (C.c_int, [_vp]),
         "edb_server_stop": (C.c_int, [_vp]),
         "edb_server_wait": (C.c_int, [_vp, C.c_longlong, C.c_double]),
+        "edb_server_cancel": (C.c_int, [_vp, C.c_longlong]),
         "edb_server_result": (C.c_int, [_vp, C.c_longlong, _dp, _dp, C.POINTER(RequestInfo)]),
         "edb_server_get_stats": (C.c_int, [_vp, C.POINTER(ServerStats)]),
         "edb_server_clock": (C.c_int, [_vp, _dp]),

@@ -443,6 +443,10 @@ class BatchSolver:
             out.append(Fh.reshape(self.S, self.NQ))
         return out[0] if len(out) == 1 else tuple(out)
 
+    def read_device(self, d_F_real, stream=None):
+        """Real-space f (S x N^3 float64) into a device buffer (torch tensor or address)."""
+        check(lib.edb_batch_read_device(self._h, devptr(d_F_real), stream_ptr(stream)))
+
     def moments(self):
         m = np.empty(self.S * 5)
         H = np.empty(self.S)
@@ -461,6 +465,42 @@ class BatchSolver:
                 self._h = None
         except Exception:
             pass
+
+
+class CellSolver:
+    """Spatially inhomogeneous use: df/dt + v1 df/dx = Q(f) on a periodic 1-D
+    grid of C cells [0, Lx), each cell holding a velocity distribution on
+    [-R, R]^3 (N^3 points), all sharing one ALIASED kernel table (no reference
+    counterpart: the reference solves the homogeneous equation only).
+
+    The state is a C x N^3 float64 device tensor, cells-major.  ``collide``
+    advances every cell's homogeneous collision step (a BatchSolver with one
+    solve per cell: FP32 compensated Q-hat, FP64 state), ``transport`` streams
+    freely in x (edb_cells_transport_x_device), and ``strang_step`` does
+    transport dt/2, collide dt, transport dt/2."""
+
+    def __init__(self, qcalc: QCalculator, C: int, R: float, Lx: float, scheme: int = SCHEME_RK4,
+                 dt: float = 0.01, fix_entropy: bool = False, conserve: bool = False):
+        self.C, self.N, self.R, self.Lx, self.dt = int(C), qcalc.N, float(R), float(Lx), float(dt)
+        self.batch = BatchSolver(qcalc, C, R, scheme, dt, fix_entropy=fix_entropy,
+                                 conserve=conserve)
+
+    def transport(self, d_f, d_out, dt, stream=None):
+        """d_out <- free streaming of d_f over dt (both C x N^3, distinct)."""
+        check(lib.edb_cells_transport_x_device(self.C, self.N, self.R, self.Lx, float(dt),
+                                               devptr(d_f), devptr(d_out), stream_ptr(stream)))
+
+    def collide(self, d_f, nsteps=1, stream=None):
+        """In place: every cell's distribution advanced nsteps collision steps."""
+        self.batch.load_device(d_f, stream)
+        self.batch.step(int(nsteps), stream)
+        self.batch.read_device(d_f, stream)
+
+    def strang_step(self, d_f, d_tmp, stream=None):
+        """One Strang step of length dt, in place on d_f (d_tmp: scratch of the same shape)."""
+        self.transport(d_f, d_tmp, 0.5 * self.dt, stream)
+        self.collide(d_tmp, 1, stream)
+        self.transport(d_tmp, d_f, 0.5 * self.dt, stream)
 
 
 # ---------------------------------------------------------- serving engine
@@ -518,10 +558,15 @@ class Server:
         """Block until request rid is done (timeout_s <= 0: no limit)."""
         check(lib.edb_server_wait(self._h, int(rid), float(timeout_s)))
 
+    def cancel(self, rid: int):
+        """Cancel request rid: dropped if queued, retired (slot freed) at the end
+        of its step in flight if running; wait() then raises EDB_ECANCELED."""
+        check(lib.edb_server_cancel(self._h, int(rid)))
+
     def info(self, rid: int) -> dict:
         i = RequestInfo()
         check(lib.edb_server_result(self._h, int(rid), None, None, C.byref(i)))
-        # state: 0 queued, 1 running, 2 done, 3 refused
+        # state: 0 queued, 1 running, 2 done, 3 refused, 4 cancelled, 5 failed
         return {"state": i.state, "N": i.N, "steps": i.steps, "t_arrival": i.t_arrival,
                 "t_admit": i.t_admit, "t_done": i.t_done}
 

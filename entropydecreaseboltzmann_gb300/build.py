@@ -32,6 +32,7 @@ UNITS = {
     "edb_kernels_misc.cu": ["-fmad=false"],
     "edb_noalloc.cu": [],
     "edb_server.cu": [],
+    "edb_kernels_transport.cu": [],
 }
 
 

@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <atomic>
+#include <cmath>
 #include <fstream>
 #include <iomanip>
 #include <mutex>
@@ -87,6 +88,8 @@ extern "C" const char *edb_status_string(edb_status s) {
     case EDB_ENOTREADY: return "EDB_ENOTREADY";
     case EDB_EBUSY: return "EDB_EBUSY";
     case EDB_ENOTFOUND: return "EDB_ENOTFOUND";
+    case EDB_ECANCELED: return "EDB_ECANCELED";
+    case EDB_ENONFINITE: return "EDB_ENONFINITE";
   }
   return "EDB_UNKNOWN";
 }
@@ -787,6 +790,10 @@ extern "C" edb_status edb_solver_destroy(edb_solver *s) {
 extern "C" edb_status edb_solver_set_initial(edb_solver *s, const double *F0) {
   if (!s) return fail(EDB_EINVAL, "null handle");
   if (F0)
+    for (long long i = 0; i < 2 * s->NQ; ++i)
+      if (!std::isfinite(F0[i]))
+        return fail(EDB_EINVAL, "initial data contains a NaN or an infinity");
+  if (F0)
     s->F0.assign(F0, F0 + 2 * s->NQ);
   else
     s->F0.clear();
@@ -1346,6 +1353,16 @@ extern "C" edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat)
     EDB_CUDA(cudaStreamSynchronize(b->cst));
   }
   EDB_CUDA(cudaStreamSynchronize(st));
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_batch_read_device(edb_batch *b, double *d_F_real, void *stream) {
+  if (!b || !d_F_real) return fail(EDB_EINVAL, "null argument");
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->st;
+  // F is scratch between steps (the step graph rewrites it when the fix runs)
+  EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->Fhat, b->F, nullptr, 1, 0, st));
+  EDB_TRY(launch_complex_to_real(b->n, b->F, d_F_real, st));
+  if (!stream) EDB_CUDA(cudaStreamSynchronize(st));
   return EDB_OK;
 }
 

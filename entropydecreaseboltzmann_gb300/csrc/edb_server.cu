@@ -27,6 +27,8 @@
 // Groups run concurrently on their own streams.  Each solve's arithmetic
 // depends only on its own slot, so a result is the same alone and in a mix.
 #include <math.h>
+
+#include <cmath>
 #include <string.h>
 
 #include <algorithm>
@@ -53,7 +55,10 @@ struct Req {
   edb_request r;
   std::vector<double> F0;
   double t_arrival = -1, t_admit = -1, t_done = -1;
-  int state = 0;  // 0 queued / not arrived, 1 running, 2 done, 3 refused (cannot fit)
+  // 0 queued / not arrived, 1 running, 2 done, 3 refused (cannot fit),
+  // 4 cancelled, 5 failed (its state became non-finite)
+  int state = 0;
+  bool cancel = false;  // running: retire at the next step boundary without a result
   int group = -1;
   int remaining = 0;
   std::vector<double> F, Fhat;  // results (want_result)
@@ -115,6 +120,7 @@ struct edb_server {
   long long bytes_used = 0;
   double bytes_peak = 0;
   long long steps_launched = 0, launches = 0, completed = 0, refused = 0;
+  long long cancelled = 0, failed = 0;
   double evals = 0, evals_padded = 0;
   // every field above is guarded by mu once the background loop runs
   std::mutex mu;
@@ -132,6 +138,11 @@ namespace {
 double now_s(const edb_server *s) {
   if (!s->clock_started) return 0.0;
   return std::chrono::duration<double>(Clock::now() - s->t0).count();
+}
+
+// Requests that need no more work (done, refused, cancelled or failed).
+long long settled(const edb_server *s) {
+  return s->completed + s->refused + s->cancelled + s->failed;
 }
 
 // Chunk count of the batched kernel for a table of N (fixed per N).
@@ -493,7 +504,7 @@ edb_status complete(edb_server *s, Group &g) {
   std::vector<int> fin;
   for (int i = 0; i < g.inflight_live; ++i) {
     Req &r = s->reqs[(size_t)g.slot_req[(size_t)i]];
-    if (--r.remaining <= 0) fin.push_back(i);
+    if (--r.remaining <= 0 || r.cancel) fin.push_back(i);  // finished or cancelled
   }
   if (fin.empty()) return EDB_OK;
   const size_t NQ = (size_t)g.NQ;
@@ -516,6 +527,20 @@ edb_status complete(edb_server *s, Group &g) {
     const double t = now_s(s);
     for (int j = 0; j < k; ++j) {
       Req &r = s->reqs[(size_t)g.slot_req[(size_t)fin[c0 + (size_t)j]]];
+      r.t_done = t;
+      if (r.cancel) {  // its slot is freed; no result
+        r.state = 4;
+        ++s->cancelled;
+        continue;
+      }
+      // a solve whose state overflowed or became NaN is reported as failed
+      bool finite = true;
+      for (size_t i = 0; i < NQ && finite; ++i) finite = std::isfinite(g.h_F[(size_t)j * NQ + i].x);
+      if (!finite) {
+        r.state = 5;
+        ++s->failed;
+        continue;
+      }
       if (r.r.want_result) {
         r.F.resize(NQ);
         for (size_t i = 0; i < NQ; ++i) r.F[i] = g.h_F[(size_t)j * NQ + i].x;
@@ -523,7 +548,6 @@ edb_status complete(edb_server *s, Group &g) {
                       (const double *)(g.h_Fhat + (size_t)(j + 1) * NQ));
       }
       r.state = 2;
-      r.t_done = t;
       ++s->completed;
     }
     s->cv_done.notify_all();
@@ -637,6 +661,10 @@ extern "C" edb_status edb_server_submit(edb_server *s, const edb_request *r, con
   if (!(r->gamma >= 0 && r->gamma <= 2)) return fail(EDB_EINVAL, "gamma must be in [0, 2]");
   if (r->steps < 1) return fail(EDB_EINVAL, "steps must be >= 1");
   const long long NQ = (long long)r->N * r->N * r->N;
+  for (long long i = 0; i < NQ; ++i)
+    if (!std::isfinite(F0_real[i]))
+      return fail(EDB_EINVAL, "initial data contains a NaN or an infinity (entry " +
+                                  std::to_string(i) + ")");
   if (table_bytes_of(r->N) + fixed_bytes_of(r->N) + BUCKET * slot_bytes(s, r->N) >
       (long long)s->d.hbm_budget_bytes)
     return fail(EDB_ENOMEM, "request cannot fit the HBM budget");
@@ -670,6 +698,10 @@ edb_status iterate(edb_server *s, bool *busy, bool *stuck) {
     const long long id = s->pending[s->pending_head];
     Req &r = s->reqs[(size_t)id];
     if (r.t_arrival > now) break;
+    if (r.state == 4) {  // cancelled before it arrived
+      ++s->pending_head;
+      continue;
+    }
     int gi = 0;
     EDB_TRY(get_group(s, r.r.N, r.r.gamma, r.r.R, &gi));
     s->groups[(size_t)gi]->queue.push_back(id);
@@ -771,7 +803,7 @@ extern "C" edb_status edb_server_run(edb_server *s, double max_wall_s) {
   for (;;) {
     bool busy = false, stuck = false;
     EDB_TRY(iterate(s, &busy, &stuck));
-    if (s->completed + s->refused == (long long)s->reqs.size()) break;
+    if (settled(s) == (long long)s->reqs.size()) break;
     if (max_wall_s > 0 && now_s(s) - t_start > max_wall_s) break;
     if (stuck) return fail(EDB_ENOMEM, "queued requests cannot be admitted within the HBM budget");
     lk.unlock();
@@ -835,7 +867,37 @@ extern "C" edb_status edb_server_wait(edb_server *s, long long id, double timeou
   if (s->loop_status != EDB_OK) return fail(s->loop_status, s->loop_msg);
   const int st = s->reqs[(size_t)id].state;
   if (st == 3) return fail(EDB_ENOMEM, "request refused: it cannot fit the HBM budget");
+  if (st == 4) return fail(EDB_ECANCELED, "request cancelled");
+  if (st == 5) return fail(EDB_ENONFINITE, "the solve's state became non-finite");
   if (st != 2) return fail(EDB_ENOTREADY, "the loop stopped before the request finished");
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_server_cancel(edb_server *s, long long id) {
+  if (!s) return fail(EDB_EINVAL, "null handle");
+  std::unique_lock<std::mutex> lk(s->mu);
+  if (id < 0 || id >= (long long)s->reqs.size()) return fail(EDB_ENOTFOUND, "unknown request");
+  Req &r = s->reqs[(size_t)id];
+  if (r.state == 1) {  // running: retired (slot freed) when its step in flight ends
+    r.cancel = true;
+    return EDB_OK;
+  }
+  if (r.state != 0) return fail(EDB_EINVAL, "request already finished");
+  // queued in its group (arrived) or still pending (not arrived)
+  for (auto &g : s->groups) {
+    auto it = std::find(g->queue.begin(), g->queue.end(), id);
+    if (it != g->queue.end()) {
+      g->queue.erase(it);
+      break;
+    }
+  }
+  r.state = 4;
+  r.t_done = now_s(s);
+  std::vector<double>().swap(r.F0);
+  ++s->cancelled;
+  lk.unlock();
+  s->cv_done.notify_all();
+  s->cv_work.notify_one();
   return EDB_OK;
 }
 
@@ -914,5 +976,7 @@ extern "C" edb_status edb_server_get_stats(edb_server *s, edb_server_stats *o) {
   o->hbm_bytes_peak = s->bytes_peak;
   o->groups = (int)s->groups.size();
   o->refused = s->refused;
+  o->cancelled = s->cancelled;
+  o->failed = s->failed;
   return EDB_OK;
 }

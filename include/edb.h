@@ -43,7 +43,9 @@ typedef enum {
   EDB_ETIMEDOUT = 4,  /* a bounded device wait ran out */
   EDB_ENOTREADY = 5,  /* state not initialised (e.g. calQ before genB) */
   EDB_EBUSY = 6,      /* resource in use (e.g. server slots full) */
-  EDB_ENOTFOUND = 7   /* unknown request id */
+  EDB_ENOTFOUND = 7,  /* unknown request id */
+  EDB_ECANCELED = 8,  /* the request was cancelled (edb_server_cancel) */
+  EDB_ENONFINITE = 9  /* a solve's state became non-finite (NaN or infinity) */
 } edb_status;
 
 /* Index modes of the collision sum.
@@ -280,7 +282,8 @@ typedef struct edb_solver edb_solver;
 edb_status edb_solver_create(const edb_solver_desc *d, edb_solver **out);
 edb_status edb_solver_destroy(edb_solver *s);
 /* Initial data in real space (N^3 interleaved complex); NULL selects the
- * reference's setInitialValue (BKW.h:121-138, the live funExact branch). */
+ * reference's setInitialValue (BKW.h:121-138, the live funExact branch).
+ * EDB_EINVAL when it holds a NaN or an infinity. */
 edb_status edb_solver_set_initial(edb_solver *s, const double *F0);
 /* Runs the reference loop `do { t += dt; ... } while (t < TEnd)` of the
  * chosen scheme from T0 (BKW.h:218-248 etc.), entirely on the device: calQ
@@ -327,6 +330,9 @@ edb_status edb_batch_step(edb_batch *b, int nsteps, void *stream);
 /* Real-space f (S x N^3 doubles) and Fhat (S x N^3 complex) to host memory;
  * either pointer may be NULL. */
 edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat);
+/* Real-space f (S x N^3 doubles) into device memory, stream-ordered (NULL:
+ * the batch's own stream, synchronous). */
+edb_status edb_batch_read_device(edb_batch *b, double *d_F_real, void *stream);
 /* Per-solve moments of the current state: S x 5 doubles (mass, momentum x3,
  * energy) on the velocity grid, and the entropy H (S doubles). */
 edb_status edb_batch_moments(edb_batch *b, double *moments, double *entropy);
@@ -369,7 +375,8 @@ typedef struct {
 
 typedef struct {
   int state;          /* 0 queued, 1 running, 2 done, 3 refused (its table and slots could
-                         not be fitted in the budget while nothing else ran) */
+                         not be fitted in the budget while nothing else ran), 4 cancelled,
+                         5 failed (its state became non-finite; no result kept) */
   int N, steps;
   double t_arrival, t_admit, t_done; /* server clock, seconds (-1: not yet) */
 } edb_request_info;
@@ -388,6 +395,8 @@ typedef struct {
   double hbm_bytes_peak;      /* tables + arenas */
   int groups;
   long long refused;          /* requests refused by the background loop (state 3) */
+  long long cancelled;        /* requests cancelled (state 4) */
+  long long failed;           /* solves whose state became non-finite (state 5) */
 } edb_server_stats;
 
 typedef struct edb_server edb_server;
@@ -396,10 +405,16 @@ edb_status edb_server_destroy(edb_server *s);
 /* Builds the table of group (N, gamma, R) now (otherwise the first request of
  * the group pays for it). */
 edb_status edb_server_prepare(edb_server *s, int N, double gamma, double R);
-/* Queues a request; F0_real (N^3 doubles, host) is copied.  EDB_ENOMEM when
- * its table plus one slot can never fit the budget. */
+/* Queues a request; F0_real (N^3 doubles, host) is copied.  EDB_EINVAL when
+ * it holds a NaN or an infinity, EDB_ENOMEM when its table plus one slot can
+ * never fit the budget. */
 edb_status edb_server_submit(edb_server *s, const edb_request *r, const double *F0_real,
                              long long *id);
+/* Cancels a request: a queued (or not yet arrived) one is dropped at once, a
+ * running one is retired at the end of its step in flight, which frees its
+ * slot; no result is kept, and edb_server_wait reports EDB_ECANCELED.
+ * EDB_EINVAL when the request has already finished. */
+edb_status edb_server_cancel(edb_server *s, long long id);
 /* Runs the request loop on the calling thread until every submitted request
  * is done or max_wall_s seconds (<= 0: no limit) have passed (EDB_EBUSY while
  * the background loop runs). */
@@ -411,7 +426,8 @@ edb_status edb_server_run(edb_server *s, double max_wall_s);
 edb_status edb_server_start(edb_server *s);
 edb_status edb_server_stop(edb_server *s);
 /* Waits until request id is done (timeout_s <= 0: no limit): EDB_OK, or
- * EDB_ETIMEDOUT, or EDB_ENOMEM if it was refused. */
+ * EDB_ETIMEDOUT, or EDB_ENOMEM if it was refused, EDB_ECANCELED if it was
+ * cancelled, EDB_ENONFINITE if its state overflowed or became NaN. */
 edb_status edb_server_wait(edb_server *s, long long id, double timeout_s);
 /* f (N^3 doubles) and Fhat (N^3 complex) of a finished request kept with
  * want_result (either pointer may be NULL); info may be NULL. */
@@ -420,6 +436,21 @@ edb_status edb_server_result(edb_server *s, long long id, double *F_real, double
 edb_status edb_server_get_stats(edb_server *s, edb_server_stats *out);
 /* The server clock (seconds since the first edb_server_run; 0 before). */
 edb_status edb_server_clock(edb_server *s, double *t);
+
+/* ------------------------------------------- spatially inhomogeneous use */
+/* No reference counterpart (the reference solves the space-homogeneous
+ * equation only).  df/dt + v1 df/dx = Q(f) on a periodic x grid of C cells
+ * [0, Lx) splits into this transport step and one homogeneous collision
+ * step per cell (a batched solve with S = C: edb_batch_load_device, _step,
+ * _read_device).  d_f / d_out: C x N^3 doubles, cells-major (one cell's
+ * velocity distribution on the grid v_d = -R + i_d 2R/N is contiguous), on
+ * the device, distinct.  Free streaming over dt by the semi-Lagrangian rule
+ * with linear interpolation: out[c][v] = f at x_c - v1 dt, interpolated
+ * between the two upstream cells.  The weights are non-negative and sum to
+ * one per velocity, so each velocity slice's total (mass, momentum, energy)
+ * is kept to rounding and f >= 0 stays so.  Stream-ordered. */
+edb_status edb_cells_transport_x_device(int C, int N, double R, double Lx, double dt,
+                                        const double *d_f, double *d_out, void *stream);
 
 /* -------------------------------------------------------- conservation */
 /* No reference counterpart: the moment functionals of conservative mode.

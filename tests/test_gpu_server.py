@@ -227,3 +227,71 @@ def test_background_loop_serves_concurrent_clients(edb):
     st = srv.stats()
     assert st["completed"] == len(specs) + 1 and st["refused"] == 0
     srv.close()
+
+
+def test_failure_paths_free_their_slots(edb):
+    """Failures are handled on the host and free what they held; nothing on
+    the device faults:
+    * initial data with a NaN is refused at submit (EDB_EINVAL) and never
+      queued;
+    * a queued request that is cancelled never runs (EDB_ECANCELED from wait);
+    * a running request that is cancelled is retired at the end of its step
+      in flight: its slot is freed and the group's live count drops to 0;
+    * a solve whose state overflows (initial data of 1e300 per cell) is
+      reported as failed (EDB_ENONFINITE) and its slot freed;
+    * the loop keeps serving: a request submitted afterwards completes and
+      equals the same solve alone."""
+    import time
+
+    from entropydecreaseboltzmann_gb300 import data
+
+    N, R = 12, 6.0
+    f = data.maxwellian_mixture_batch(1, N, R, seed=21)[0]
+    bad = f.copy()
+    bad[7] = np.nan
+    srv = edb.Server(hbm_budget_bytes=8e9, scheme=edb.SCHEME_RK4, dt=0.01)
+    srv.prepare(N, 0.0, R)
+    with pytest.raises(edb.EdbError) as e:
+        srv.submit(N, 0.0, R, 5, bad)
+    assert e.value.status == 1
+    assert srv.stats()["submitted"] == 0
+
+    srv.start()
+    try:
+        # cancelled while queued: arrives far in the future, never runs
+        late = srv.submit(N, 0.0, R, 5, f, arrival_s=1e6)
+        srv.cancel(late)
+        with pytest.raises(edb.EdbError) as e:
+            srv.wait(late, timeout_s=30)
+        assert e.value.status == 8
+        # cancelled while running
+        long_id = srv.submit(N, 0.0, R, 10 ** 6, f)
+        t0 = time.time()
+        while srv.info(long_id)["state"] != 1:
+            assert time.time() - t0 < 30
+            time.sleep(0.01)
+        srv.cancel(long_id)
+        with pytest.raises(edb.EdbError) as e:
+            srv.wait(long_id, timeout_s=30)
+        assert e.value.status == 8
+        # a state that overflows
+        boom = srv.submit(N, 0.0, R, 3, np.full(N ** 3, 1e300))
+        with pytest.raises(edb.EdbError) as e:
+            srv.wait(boom, timeout_s=30)
+        assert e.value.status == 9
+        assert srv.info(boom)["state"] == 5
+        # still serving
+        ok = srv.submit(N, 0.0, R, 5, f, want_result=True)
+        srv.wait(ok, timeout_s=60)
+    finally:
+        srv.stop()
+    st = srv.stats()
+    assert (st["cancelled"], st["failed"], st["completed"], st["live"], st["queued"]) == (2, 1, 1, 0, 0)
+    F_ok, _ = srv.result(ok)
+    srv.close()
+    alone = edb.Server(hbm_budget_bytes=8e9, scheme=edb.SCHEME_RK4, dt=0.01)
+    rid = alone.submit(N, 0.0, R, 5, f, want_result=True)
+    alone.run()
+    F_alone, _ = alone.result(rid)
+    alone.close()
+    assert rel_l2(F_ok, F_alone) <= 1e-12
