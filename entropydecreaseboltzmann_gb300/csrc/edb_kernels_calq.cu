@@ -659,6 +659,130 @@ __device__ __forceinline__ void compute_line_pair(const C32Geom &g, const float 
   }
 }
 
+// compute_line and compute_line_pair for N % A == 0 on the tensor-copy path:
+// the same operations in the same order (so the same bits), with the shared-
+// memory addresses built once per group of A l3 steps.  At group gg the
+// ring's base index (k3_0 - gg A) mod N is a multiple of A, so for t >= 1 the
+// new ring entry sits at qq - t with qq = base (N when base = 0) and needs no
+// wrap; the B-tile row pointer advances by one row pitch per l3 step.  With
+// the per-step index wrap and the row multiply gone, fewer integer
+// multiply-adds compete with the packed math for the FMA pipe.
+template <int A>
+__device__ __forceinline__ void compute_line_al(const C32Geom &g, const float *Bt,
+                                                const float2 *fl0, const float2 *fl1,
+                                                const float2 *p0, const float2 *p1, int k3_0,
+                                                u64 (&accA)[A][SC], u64 (&accB)[A][SC]) {
+  const int N = g.N;
+  const uint32_t sp0 = s_addr(p0), sp1 = s_addr(p1);
+  uint32_t sf0 = s_addr(fl0), sf1 = s_addr(fl1), bB = s_addr(Bt);
+  const uint32_t brow = 4u * g.BROW;
+  u64 ring[A][SC];
+  {
+    const uint32_t a0 = sp0 + 8u * k3_0, a1 = sp1 + 8u * k3_0;
+#pragma unroll
+    for (int a = 0; a < A; ++a) {
+      ring[a][0] = lds_u64(a0 + 8u * a);
+      ring[a][1] = lds_u64(a1 + 8u * a);
+    }
+  }
+  int base = k3_0;
+  for (int gg = 0; gg < g.R; ++gg) {
+    const int qq = base == 0 ? N : base;
+    const uint32_t t0a = sp0 + 8u * base, t0b = sp1 + 8u * base;
+    const uint32_t qa = sp0 + 8u * qq, qb = sp1 + 8u * qq;
+#pragma unroll
+    for (int t = 0; t < A; ++t) {
+      if (t > 0) {
+        ring[(A - t) % A][0] = lds_u64(qa - 8u * t);
+        ring[(A - t) % A][1] = lds_u64(qb - 8u * t);
+      } else if (gg > 0) {
+        ring[0][0] = lds_u64(t0a);
+        ring[0][1] = lds_u64(t0b);
+      }
+      float bv[A];
+#pragma unroll
+      for (int q4 = 0; q4 < A / 4; ++q4) {
+        const float4 b = lds_f4(bB + 16u * q4);
+        bv[4 * q4] = b.x;
+        bv[4 * q4 + 1] = b.y;
+        bv[4 * q4 + 2] = b.z;
+        bv[4 * q4 + 3] = b.w;
+      }
+      bB += brow;
+      const float2 f0 = lds_f2(sf0 + 8u * t), f1 = lds_f2(sf1 + 8u * t);
+      const u64 flx[SC] = {pk(f0.x, f0.x), pk(f1.x, f1.x)};
+      const u64 fly[SC] = {pk(f0.y, f0.y), pk(f1.y, f1.y)};
+#pragma unroll
+      for (int a = 0; a < A; ++a) {
+        const int slot = (a - t + A) % A;
+        const u64 bb = pk(bv[a], bv[a]);
+#pragma unroll
+        for (int c = 0; c < SC; ++c) {
+          const u64 q = mul2(bb, ring[slot][c]);
+          fma2(accA[a][c], flx[c], q);
+          fma2(accB[a][c], fly[c], q);
+        }
+      }
+    }
+    sf0 += 8u * A;
+    sf1 += 8u * A;
+    base -= A;
+    if (base < 0) base += N;
+  }
+}
+
+template <int A>
+__device__ __forceinline__ void compute_line_pair_al(const C32Geom &g, const float *Bt,
+                                                     const float2 *fl, const float2 *p, int k3_0,
+                                                     u64 (&accA)[A][SC], u64 (&accB)[A][SC]) {
+  const int N = g.N;
+  const uint32_t sp = s_addr(p);
+  uint32_t sf = s_addr(fl), bB = s_addr(Bt);
+  const uint32_t brow = 4u * g.BROW;
+  ulonglong2 ring[A];
+  {
+    const uint32_t a0 = sp + 16u * k3_0;
+#pragma unroll
+    for (int a = 0; a < A; ++a) ring[a] = lds_u64x2(a0 + 16u * a);
+  }
+  int base = k3_0;
+  for (int gg = 0; gg < g.R; ++gg) {
+    const int qq = base == 0 ? N : base;
+    const uint32_t t0 = sp + 16u * base, qa = sp + 16u * qq;
+#pragma unroll
+    for (int t = 0; t < A; ++t) {
+      if (t > 0)
+        ring[(A - t) % A] = lds_u64x2(qa - 16u * t);
+      else if (gg > 0)
+        ring[0] = lds_u64x2(t0);
+      float bv[A];
+#pragma unroll
+      for (int q4 = 0; q4 < A / 4; ++q4) {
+        const float4 b = lds_f4(bB + 16u * q4);
+        bv[4 * q4] = b.x;
+        bv[4 * q4 + 1] = b.y;
+        bv[4 * q4 + 2] = b.z;
+        bv[4 * q4 + 3] = b.w;
+      }
+      bB += brow;
+      const ulonglong2 f = lds_u64x2(sf + 16u * t);
+#pragma unroll
+      for (int a = 0; a < A; ++a) {
+        const ulonglong2 m = ring[(a - t + A) % A];
+        const u64 bb = pk(bv[a], bv[a]);
+        const u64 qr = mul2(bb, m.x), qi = mul2(bb, m.y);
+        fma2(accA[a][0], f.x, qr);
+        fma2(accA[a][1], f.x, qi);
+        fma2(accB[a][0], f.y, qr);
+        fma2(accB[a][1], f.y, qi);
+      }
+    }
+    sf += 16u * A;
+    base -= A;
+    if (base < 0) base += N;
+  }
+}
+
 // Solve pairs for the PAIR variants: out[P][e] = (re_2P, re_2P+1, im_2P,
 // im_2P+1); a missing odd partner reads as zero.
 __global__ void c32_pairs_kernel(int S, long long NQ, const float2 *__restrict__ fin,
@@ -747,6 +871,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
   const int nlines = nplanes * N;
   auto line_li = [&](int j) { return plane_l1(P0 + j / N) * N + j % N; };
   const size_t plane_sz = (size_t)g.SG * g.PSTR;
+  const bool ring_al = (N % A) == 0;  // compute_line*_al apply (tensor-copy path)
 
   // zero the tile/line buffers once: padded rows (l3 >= N), row tails and the
   // f_l tails are never written by the copies and must read as zeros
@@ -860,14 +985,18 @@ __global__ void __launch_bounds__(MAXT, MINB)
     const float2 *fl0 = fls + (size_t)st * g.FSTG + (size_t)w * g.FLS;
     const float2 *p0 = plb + (size_t)pb * plane_sz + (size_t)w * g.PSTR + m2 * N * g.EL;
     if (PAIR) {
-      if (TMA)
+      if (TMA && ring_al)
+        compute_line_pair_al<A>(g, Bt, fl0, p0, k3_0, accA, accB);
+      else if (TMA)
         compute_line_pair<true, true, A>(g, Bt, fl0, p0, k3_0, accA, accB);
       else
         compute_line_pair<false, false, A>(g, Bt, fl0, p0, k3_0, accA, accB);
     } else {
       const float2 *fl1 = fl0 + (size_t)WS * g.FLS;
       const float2 *p1 = p0 + (size_t)WS * g.PSTR;
-      if (TMA)
+      if (TMA && ring_al)
+        compute_line_al<A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
+      else if (TMA)
         compute_line<true, true, A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
       else
         compute_line<false, false, A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
