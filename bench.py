@@ -276,6 +276,10 @@ def main():
     ap.add_argument("--probe-S", type=int, default=256)
     ap.add_argument("--probe-L", type=float, default=7.0)
     ap.add_argument("--probe-mode", type=int, default=1, help="calq64: index mode")
+    ap.add_argument("--probe-kernel", type=int, default=0,
+                    help="calq64: FP64 kernel (0 double-float streamed, 1 native, 2 on the fly)")
+    ap.add_argument("--probe-compact", action="store_true",
+                    help="calq64: build only the compact tables (genB_compact)")
     ap.add_argument("--probe-reps", type=int, default=2)
     ap.add_argument("--probe-variant", type=int, default=-1,
                     help="calq32: this kernel variant instead of the autotuned one")
@@ -563,7 +567,11 @@ def probe(args):
         terms = float(N) ** 6 * S
     else:
         q = edb.QCalculator(N, 0, L=L, filter=False, index_mode=args.probe_mode)
-        q.genB()
+        if args.probe_compact:
+            q.genB_compact()
+        else:
+            q.genB()
+            q.set_fp64_kernel(args.probe_kernel)
         f = data.bkw_grid(N, L, 5.5)
         fin = torch.from_numpy(np.fft.fftn(f.reshape(N, N, N)).reshape(-1)).cuda()
         out = torch.empty_like(fin)

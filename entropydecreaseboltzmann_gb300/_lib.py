@@ -23,7 +23,7 @@ INDEX_REFERENCE = 0
 INDEX_ALIASED = 1
 R_REFERENCE = 6.62132
 SCHEME_FE, SCHEME_CFE, SCHEME_RK2, SCHEME_SSP3, SCHEME_RK4, SCHEME_DUFORT = range(6)
-FP64_EMULATED, FP64_NATIVE = 0, 1
+FP64_EMULATED, FP64_NATIVE, FP64_ONTHEFLY = 0, 1, 2
 
 
 class EdbError(RuntimeError):
@@ -106,6 +106,7 @@ def _load():
         "edb_qcalc_destroy": (C.c_int, [_vp]),
         "edb_qcalc_close_filter": (C.c_int, [_vp]),
         "edb_qcalc_genB": (C.c_int, [_vp]),
+        "edb_qcalc_genB_compact": (C.c_int, [_vp]),
         "edb_qcalc_calQ": (C.c_int, [_vp, _dp, _dp]),
         "edb_qcalc_calQ_device": (C.c_int, [_vp, _vp, _vp, _vp]),
         "edb_qcalc_calQ_batch_f32_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),

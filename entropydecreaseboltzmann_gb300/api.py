@@ -81,6 +81,11 @@ class QCalculator:
     def genB(self):
         check(lib.edb_qcalc_genB(self._h))
 
+    def genB_compact(self):
+        """genB without the N^6 table: only the small tables the on-the-fly
+        FP64 kernel reads (aliased index shifts: ALIASED mode or odd N)."""
+        check(lib.edb_qcalc_genB_compact(self._h))
+
     def funF(self, xi, eta):
         """funF(xi, eta) (QCalculator.h:76-106) for this calculator's alpha,
         evaluated on the device; scalars or arrays."""
@@ -127,7 +132,8 @@ class QCalculator:
                                               stream_ptr(stream)))
 
     def set_fp64_kernel(self, kind):
-        """0 = FP64-accurate double-float on the FP32 pipe (default), 1 = native FP64."""
+        """0 = FP64-accurate double-float on the FP32 pipe (default), 1 = native FP64,
+        2 = double-float with the pair entries formed on the fly (no N^6 table)."""
         check(lib.edb_qcalc_set_fp64_kernel(self._h, int(kind)))
 
     def autotune_batch(self, S, d_fin, d_Q, stream=None):

@@ -26,6 +26,7 @@ UNITS = {
     "edb_capi.cu": [],
     "edb_kernels_calq.cu": [],
     "edb_kernels_calq64x.cu": [],
+    "edb_kernels_calq64f.cu": [],
     "edb_kernels_conserve.cu": [],
     "edb_kernels_fft.cu": [],
     "edb_kernels_genb.cu": ["-fmad=false"],

@@ -4,6 +4,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <fstream>
@@ -116,6 +117,11 @@ struct edb_qcalc {
   float2 *B2 = nullptr;     // B64 split into (hi, lo) floats, same layout
   float *B32 = nullptr;     // FP32 pair table, visited planes only (c32_table_floats; ALIASED)
   float4 *fdf = nullptr;    // input split for the double-float kernel
+  // tables of the on-the-fly FP64 kernel (aliased index shifts): T rval split
+  // (compressed over b = a mod 4) and {Bmm, sigma3} per mode
+  float2 *tc = nullptr;
+  float4 *bs = nullptr;
+  int amax = 0;
   int fp64_kernel = EDB_FP64_EMULATED;
   int c64x_minb = 2;    // register cap of the double-float kernel, tuned at genB
   double2 *partial = nullptr;
@@ -200,6 +206,8 @@ extern "C" edb_status edb_qcalc_destroy(edb_qcalc *q) {
   dfree(q->B2);
   dfree(q->B32);
   dfree(q->fdf);
+  dfree(q->tc);
+  dfree(q->bs);
   dfree(q->pairs);
   dfree(q->partial);
   dfree(q->fin);
@@ -239,6 +247,7 @@ static edb_status qcalc_alloc_work(edb_qcalc *q) {
     q->nchunk = calq64_nchunk(q->p);
     int nmax = calq64x_nchunk(q->p, nullptr);
     if (q->nchunk > nmax) nmax = q->nchunk;
+    if (qcalc_b2_paired(q)) nmax = std::max(nmax, calq64f_nchunk(q->p));
     EDB_TRY(dalloc(&q->partial, (size_t)nmax * q->p.KC));
   }
 
@@ -287,6 +296,18 @@ static edb_status qcalc_tune_fp64(edb_qcalc *q) {
   return check_device_waits("genB (FP64 kernel timing)");
 }
 
+// The on-the-fly kernel's tables from the FP64 F-table, sigma and Bmm.
+static edb_status qcalc_build_compact(edb_qcalc *q, const double *T, const double *sigma,
+                                      const double *Bmm) {
+  const int N = q->d.N;
+  q->amax = amax_of(N);
+  if (!q->tc)
+    EDB_TRY(dalloc(&q->tc, (size_t)(q->amax + 1) * (size_t)calq64f_row_len(q->amax)));
+  if (!q->bs) EDB_TRY(dalloc(&q->bs, (size_t)q->p.NQ));
+  return launch_calq64f_tables(N, q->d.filter, genb_rval(N, q->d.gamma, q->d.L), T, q->amax,
+                               sigma, Bmm, q->tc, q->bs, q->st);
+}
+
 extern "C" edb_status edb_qcalc_genB(edb_qcalc *q) {
   if (!q) return fail(EDB_EINVAL, "null handle");
   const int N = q->d.N;
@@ -310,6 +331,7 @@ extern "C" edb_status edb_qcalc_genB(edb_qcalc *q) {
     s = launch_genB(N, q->d.gamma, q->d.L, q->d.filter, q->d.index_mode, T, amax, sigma, Bmm,
                     q->B64, q->B32, q->st);
   if (s == EDB_OK) s = qcalc_split_B2(q);
+  if (s == EDB_OK && qcalc_b2_paired(q)) s = qcalc_build_compact(q, T, sigma, Bmm);
   cudaError_t e = cudaStreamSynchronize(q->st);
   dfree(T);
   dfree(sigma);
@@ -318,6 +340,32 @@ extern "C" edb_status edb_qcalc_genB(edb_qcalc *q) {
   if (e != cudaSuccess) return cuda_fail(e, "genB");
   q->ready = true;
   return qcalc_tune_fp64(q);
+}
+
+extern "C" edb_status edb_qcalc_genB_compact(edb_qcalc *q) {
+  if (!q) return fail(EDB_EINVAL, "null handle");
+  if (!qcalc_b2_paired(q))
+    return fail(EDB_EINVAL, "the compact tables need the aliased index shifts (ALIASED, or odd N)");
+  const int N = q->d.N;
+  const int amax = amax_of(N);
+  double *T = nullptr, *sigma = nullptr, *Bmm = nullptr;
+  EDB_TRY(qcalc_alloc_work(q));
+  edb_status s = dalloc(&T, (size_t)(amax + 1) * (amax + 1));
+  if (s == EDB_OK) s = dalloc(&sigma, 64);
+  if (s == EDB_OK) s = dalloc(&Bmm, (size_t)q->p.NQ);
+  if (s == EDB_OK) s = launch_ftable(N, q->d.gamma, T, amax, q->st);
+  if (s == EDB_OK)
+    s = launch_bmm(N, q->d.gamma, q->d.L, q->d.filter, q->d.index_mode, T, amax, sigma, Bmm,
+                   q->st);
+  if (s == EDB_OK) s = qcalc_build_compact(q, T, sigma, Bmm);
+  cudaError_t e = cudaStreamSynchronize(q->st);
+  dfree(T);
+  dfree(sigma);
+  dfree(Bmm);
+  if (s != EDB_OK) return s;
+  if (e != cudaSuccess) return cuda_fail(e, "genB_compact");
+  q->ready = true;
+  return EDB_OK;
 }
 
 extern "C" edb_status edb_funF(int alpha, long long n, const double *xi, const double *eta,
@@ -401,6 +449,7 @@ long long qcalc_table_bytes(const edb_qcalc *q) {
   if (q->B64) b += e * 8;
   if (q->B2) b += e * 8;
   if (q->B32) b += c32_table_floats(q->p.N) * 4 + 256;
+  if (q->tc) b += (long long)(q->amax + 1) * calq64f_row_len(q->amax) * 8 + q->p.NQ * 16;
   return b;
 }
 }  // namespace edb
@@ -423,6 +472,7 @@ extern "C" edb_status edb_qcalc_copy_B(edb_qcalc *q, long long first, long long 
                                        double *host_out) {
   if (!q || !host_out) return fail(EDB_EINVAL, "null argument");
   if (!q->ready) return fail(EDB_ENOTREADY, "genB has not run");
+  if (!q->B64) return fail(EDB_ENOTREADY, "the full table was not built (genB_compact)");
   const long long total = q->p.NQ * q->p.NQ;
   if (first < 0 || count < 0 || first + count > total) return fail(EDB_EINVAL, "range out of table");
   EDB_CUDA(cudaMemcpy(host_out, q->B64 + first, sizeof(double) * count, cudaMemcpyDeviceToHost));
@@ -441,8 +491,14 @@ extern "C" edb_status edb_qcalc_get_info(edb_qcalc *q, edb_qcalc_info *out) {
   return EDB_OK;
 }
 
-// The FP64 collision sum with the handle's selected kernel.
+// The FP64 collision sum with the handle's selected kernel (the on-the-fly
+// one also whenever only the compact tables exist).
 static edb_status qcalc_fp64(edb_qcalc *q, const double2 *in, double2 *out, cudaStream_t st) {
+  if (q->fp64_kernel == EDB_FP64_ONTHEFLY || (!q->B64 && !q->B2)) {
+    if (!q->tc) return fail(EDB_ENOTREADY, "the on-the-fly kernel's tables were not built");
+    EDB_TRY(launch_split_f(q->p.NQ, in, q->fdf, st));
+    return launch_calq64f(q->p, q->d.filter, q->amax, q->tc, q->bs, q->fdf, q->partial, out, st);
+  }
   if (q->fp64_kernel == EDB_FP64_EMULATED && q->B2) {
     EDB_TRY(launch_split_f(q->p.NQ, in, q->fdf, st));
     return launch_calq64x(q->p, q->B2, q->fdf, q->partial, out, st, q->c64x_minb,
@@ -453,7 +509,8 @@ static edb_status qcalc_fp64(edb_qcalc *q, const double2 *in, double2 *out, cuda
 
 extern "C" edb_status edb_qcalc_set_fp64_kernel(edb_qcalc *q, int kind) {
   if (!q) return fail(EDB_EINVAL, "null handle");
-  if (kind != EDB_FP64_EMULATED && kind != EDB_FP64_NATIVE) return fail(EDB_EINVAL, "unknown kind");
+  if (kind != EDB_FP64_EMULATED && kind != EDB_FP64_NATIVE && kind != EDB_FP64_ONTHEFLY)
+    return fail(EDB_EINVAL, "unknown kind");
   q->fp64_kernel = kind;
   return EDB_OK;
 }
@@ -1093,6 +1150,9 @@ struct edb_batch {
   // copy of one chunk overlaps the transforms of the next
   cudaStream_t cst = nullptr;
   cudaEvent_t xev[8] = {};
+  // NULL-stream device calls: the batch's own (non-blocking) stream first
+  // waits for the work the caller queued on the default stream
+  cudaEvent_t join_ev = nullptr;
 };
 
 static constexpr int BATCH_XFER_CHUNKS = 8;
@@ -1120,6 +1180,9 @@ extern "C" edb_status edb_batch_create(edb_qcalc *q, const edb_batch_desc *d, ed
   for (int i = 0; i < BATCH_XFER_CHUNKS && rc == EDB_OK; ++i)
     if ((e = cudaEventCreateWithFlags(&b->xev[i], cudaEventDisableTiming)) != cudaSuccess)
       rc = cuda_fail(e, "cudaEventCreate");
+  if (rc == EDB_OK &&
+      (e = cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming)) != cudaSuccess)
+    rc = cuda_fail(e, "cudaEventCreate");
   if (rc == EDB_OK) rc = dalloc(&b->Fhat, n);
   if (rc == EDB_OK) rc = dalloc(&b->F, n);
   const int nstage = d->scheme == EDB_SCHEME_RK4 ? 3 : (d->scheme == EDB_SCHEME_SSP3 ? 2 : 0);
@@ -1166,6 +1229,7 @@ extern "C" edb_status edb_batch_destroy(edb_batch *b) {
   dfree(b->m0);
   for (auto &ev : b->xev)
     if (ev) cudaEventDestroy(ev);
+  if (b->join_ev) cudaEventDestroy(b->join_ev);
   if (b->cst) cudaStreamDestroy(b->cst);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
@@ -1227,8 +1291,18 @@ extern "C" edb_status edb_batch_load(edb_batch *b, const double *F0_real) {
   return batch_init_state(b, b->st, true);
 }
 
+// With a NULL stream the device-pointer calls run on the batch's own stream,
+// which does not order against the default stream by itself: it first waits
+// for what the caller queued there (e.g. the kernel that wrote the input).
+static edb_status batch_join_default(edb_batch *b) {
+  EDB_CUDA(cudaEventRecord(b->join_ev, cudaStreamLegacy));
+  EDB_CUDA(cudaStreamWaitEvent(b->st, b->join_ev, 0));
+  return EDB_OK;
+}
+
 extern "C" edb_status edb_batch_load_device(edb_batch *b, const double *d_F0_real, void *stream) {
   if (!b || !d_F0_real) return fail(EDB_EINVAL, "null argument");
+  if (!stream) EDB_TRY(batch_join_default(b));
   cudaStream_t st = stream ? (cudaStream_t)stream : b->st;
   EDB_TRY(launch_real_to_complex(b->n, d_F0_real, b->F, st));
   return batch_init_state(b, st);
@@ -1358,6 +1432,7 @@ extern "C" edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat)
 
 extern "C" edb_status edb_batch_read_device(edb_batch *b, double *d_F_real, void *stream) {
   if (!b || !d_F_real) return fail(EDB_EINVAL, "null argument");
+  if (!stream) EDB_TRY(batch_join_default(b));
   cudaStream_t st = stream ? (cudaStream_t)stream : b->st;
   // F is scratch between steps (the step graph rewrites it when the fix runs)
   EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->Fhat, b->F, nullptr, 1, 0, st));

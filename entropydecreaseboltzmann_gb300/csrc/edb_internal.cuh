@@ -89,6 +89,23 @@ edb_status launch_genB(int N, double gamma, double L, int filter, int mode, cons
                        int amax, const double *d_sigma, const double *d_Bmm, double *d_B64,
                        float *d_B32, cudaStream_t st);
 
+// rval (the kernel scale) of an N-mode table with box half-width L.
+double genb_rval(int N, double gamma, double L);
+
+// FP64-accurate calQ with the pair entries formed on the fly (no N^6 table):
+// tc = T(a, b) rval split, row a, column q for b = (a mod 4) + 4q
+// ((amax + 1) x calq64f_row_len(amax) float2); bs = {Bmm, sigma3} split per
+// mode in FFTW order (N^3 float4).  Aliased index shifts only.  d_partial
+// holds calq64f_nchunk(p) * KC.
+int calq64f_nchunk(const QParams &p);
+int calq64f_row_len(int amax);
+edb_status launch_calq64f_tables(int N, int filter, double rval, const double *d_T, int amax,
+                                 const double *d_sigma, const double *d_Bmm, float2 *d_tc,
+                                 float4 *d_bs, cudaStream_t st);
+edb_status launch_calq64f(const QParams &p, int filter, int amax, const float2 *d_tc,
+                          const float4 *d_bs, const float4 *d_fdf, double2 *d_partial,
+                          double2 *d_Q, cudaStream_t st);
+
 // QCalculator::funF (alpha 0/1 closed forms, other alpha -> 0) and
 // ::filtering at n points.
 edb_status launch_funF_points(int alpha, long long n, const double *d_xi, const double *d_eta,

@@ -45,64 +45,14 @@
 #include <map>
 #include <mutex>
 
+#include "edb_df.cuh"
 #include "edb_internal.cuh"
 
 namespace edb {
 
 namespace {
-typedef unsigned long long u64;
+using namespace df;
 constexpr int RUN = 4;  // outputs per thread along j3
-
-__device__ __forceinline__ u64 pk(float a, float b) {
-  u64 r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-  return r;
-}
-__device__ __forceinline__ float2 upk(u64 v) {
-  float2 r;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
-  return r;
-}
-__device__ __forceinline__ u64 mul2(u64 a, u64 b) {
-  u64 d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ u64 fma2(u64 a, u64 b, u64 c) {
-  u64 d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-__device__ __forceinline__ u64 add2(u64 a, u64 b) {
-  u64 d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ u64 sub2(u64 a, u64 b) {
-  u64 d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-
-struct DF2 {  // packed double-float pair: lanes (re, im)
-  u64 h, l;
-};
-
-// acc += s * u for a real double-float scalar s (given as the pairs (s_h, s_h),
-// (-s_h, -s_h), (-s_l, -s_l)) and u = -nu_h + uc.
-__device__ __forceinline__ void df_axpy(DF2 &acc, u64 sh2, u64 nsh2, u64 nsl2, u64 nu_h, u64 uc) {
-  // leading product s_h * u_h = s_h * (-nu_h): nph = -(s_h u_h) rounded, pe exact error
-  const u64 nph = mul2(sh2, nu_h);       // = -rn(s_h u_h)
-  const u64 pe = fma2(nsh2, nu_h, nph);  // = s_h u_h - rn(s_h u_h)
-  // cross terms s_h * uc + s_l * u_h  (u_h = -nu_h, so s_l u_h = (-s_l) nu_h)
-  const u64 pl = fma2(sh2, uc, fma2(nsl2, nu_h, pe));
-  // two-sum of acc.h and p_h = -nph
-  const u64 s = sub2(acc.h, nph);
-  const u64 bb = sub2(s, acc.h);  // ~ p_h
-  const u64 e = sub2(sub2(acc.h, sub2(s, bb)), add2(nph, bb));  // (acc.h - (s - bb)) + (p_h - bb)
-  acc.h = s;
-  acc.l = add2(acc.l, add2(e, pl));
-}
 
 constexpr int DEPTH = 8;  // B rows in flight per warp
 // Limit of the drain after a wait ran out: lane 0 then waits this long at

@@ -130,6 +130,11 @@ static void gauss_legendre(int G, double *x, double *w) {
 
 static double lambda_pi() { return 2. / (3. + sqrt(2.)) * M_PI; }
 
+// rval of QCalculator::genB (QCalculator.h:176) with the box half-width L.
+double genb_rval(int N, double gamma, double L) {
+  return (4. * M_PI) * pow(2. * lambda_pi() / M_PI * L / N, 3 + gamma);
+}
+
 edb_status launch_ftable(int N, double gamma, double *d_T, int amax, cudaStream_t st) {
   (void)N;
   const double lp = lambda_pi();

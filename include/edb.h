@@ -213,7 +213,21 @@ edb_status edb_set_wait_limit_ns(long long ns);
  * bandwidth.  NATIVE: the same sum with FP64 FMA.  No reference counterpart. */
 #define EDB_FP64_EMULATED 0
 #define EDB_FP64_NATIVE 1
+/* ONTHEFLY: the double-float kernel with the pair entries formed per term from
+ * the compact tables (no N^6 table read; aliased index shifts only, i.e.
+ * ALIASED mode or odd N).  Used automatically after edb_qcalc_genB_compact. */
+#define EDB_FP64_ONTHEFLY 2
 edb_status edb_qcalc_set_fp64_kernel(edb_qcalc *q, int kind);
+
+/* genB without the N^6 table (QCalculator.h:158-229 restated per term): builds
+ * only what the on-the-fly FP64 kernel reads, the F-table T(a, b) times the
+ * kernel scale, split into (hi, lo) floats and kept for b = a mod 4 only
+ * (about 19 MB at N = 32, 302 MB at N = 64, where the full FP64 table would be
+ * 8.6 GB and 550 GB), and Bmm and the filter products per mode.  The FP64
+ * calQ entry points then run EDB_FP64_ONTHEFLY; edb_qcalc_copy_B and the
+ * batched entry points report EDB_ENOTREADY.  Aliased index shifts only
+ * (ALIASED mode, or odd N); EDB_EINVAL otherwise. */
+edb_status edb_qcalc_genB_compact(edb_qcalc *q);
 
 /* Copies count entries of the FP64 B table starting at flat index first
  * (row-major [l][k], centred indices) to host memory. */
@@ -323,7 +337,9 @@ edb_status edb_batch_create(edb_qcalc *q, const edb_batch_desc *d, edb_batch **o
 edb_status edb_batch_destroy(edb_batch *b);
 /* Real-space initial data, S x N^3 doubles (real), host memory. */
 edb_status edb_batch_load(edb_batch *b, const double *F0_real);
-/* Same, device memory (S x N^3 doubles). */
+/* Same, device memory (S x N^3 doubles).  With stream = NULL it runs on the
+ * batch's own stream after the work already queued on the default stream
+ * (which may be what wrote d_F0_real), and returns when done. */
 edb_status edb_batch_load_device(edb_batch *b, const double *d_F0_real, void *stream);
 /* Advances every solve by nsteps steps (one CUDA graph launch per step). */
 edb_status edb_batch_step(edb_batch *b, int nsteps, void *stream);
@@ -331,7 +347,8 @@ edb_status edb_batch_step(edb_batch *b, int nsteps, void *stream);
  * either pointer may be NULL. */
 edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat);
 /* Real-space f (S x N^3 doubles) into device memory, stream-ordered (NULL:
- * the batch's own stream, synchronous). */
+ * the batch's own stream after the default stream's queued work,
+ * synchronous). */
 edb_status edb_batch_read_device(edb_batch *b, double *d_F_real, void *stream);
 /* Per-solve moments of the current state: S x 5 doubles (mass, momentum x3,
  * energy) on the velocity grid, and the entropy H (S doubles). */
