@@ -7,7 +7,13 @@ Tolerances
   order; the pair entry is formed in double-float arithmetic, about 2^-48
   relative, instead of being rounded once in FP64).
   Where the oracle's full table would be too large (N = 32, 48), against the
-  oracle's direct evaluation of the aliased sum at sampled modes, <= 1e-12.
+  oracle's direct evaluation of the aliased sum at sampled modes: <= 1e-12 up
+  to N = 32.  At N = 48, beyond what the reference's own loops can run (their
+  int table index overflows from N = 36), <= 1e-11: the double-float running
+  sums lose about 2^-48 per term, and the error grows with the N^3 / 2 pair
+  terms per output (measured 3.7e-12 here; the streamed double-float kernel
+  is at 1.2e-12 against native FP64 already at N = 40).  Native FP64
+  (kernel 1) stays at 1e-15 there.
 """
 import numpy as np
 import pytest
@@ -61,8 +67,9 @@ def test_onthefly_refuses_even_N_reference_mode(edb):
     assert e.value.status == 1
 
 
-@pytest.mark.parametrize("N,L,gamma", [(24, 7.0, 0.0), (32, 8.0, 1.0), (48, 8.0, 1.0)])
-def test_onthefly_at_workload_N(edb, oracle, N, L, gamma):
+@pytest.mark.parametrize("N,L,gamma,tol", [(24, 7.0, 0.0, 1e-12), (32, 8.0, 1.0, 1e-12),
+                                           (48, 8.0, 1.0, 1e-11)])
+def test_onthefly_at_workload_N(edb, oracle, N, L, gamma, tol):
     """Compact tables only (the full FP64 table would be 1.5 GB, 8.6 GB and
     98 GB): against the oracle's direct aliased sum at 64 sampled modes, on a
     two-Maxwellian mixture; at N = 24 also against the streamed kernel."""
@@ -75,7 +82,7 @@ def test_onthefly_at_workload_N(edb, oracle, N, L, gamma):
     Qf = q.calQ(None, fin)
     modes = np.random.default_rng(N).choice(N ** 3, 64, replace=False)
     Qd = oracle.direct_modes(N, fin, modes, gamma=gamma, R=L, filter=False)
-    assert rel_l2(Qf[modes], Qd) <= 1e-12
+    assert rel_l2(Qf[modes], Qd) <= tol
     if N == 24:
         qs = edb.QCalculator(N, int(gamma), gamma=gamma, L=L, filter=False,
                              index_mode=INDEX_ALIASED)
