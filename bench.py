@@ -397,11 +397,11 @@ def main():
         fh = torch.from_numpy(np.fft.fftn(f.reshape(Nf, Nf, Nf)).reshape(-1)).cuda()
         out = torch.empty_like(fh)
         res = {}
-        for kind, name in ((0, "emulated"), (1, "native")):
+        for kind, name in ((0, "emulated"), (1, "native"), (2, "onthefly")):
             q64.set_fp64_kernel(kind)
             for _ in range(2):
                 q64.calQ_device(fh, out, stream)
-            reps = 5 if kind == 0 else 3
+            reps = 3 if kind == 1 else 5
             a0 = torch.cuda.Event(enable_timing=True)
             a1 = torch.cuda.Event(enable_timing=True)
             a0.record(stream)
@@ -412,12 +412,17 @@ def main():
             t = a0.elapsed_time(a1) / reps * 1e-3
             nb = float(Nf) ** 6 * 8
             # the double-float kernel reads the ALIASED pair table on the l1
-            # planes it visits (l1 <= (k1 - l1) mod N); the native kernel all of B
-            frac = (sum(k1 // 2 + 1 + max(0, (k1 + Nf) // 2 - k1) for k1 in range(Nf)) / Nf ** 2
-                    if kind == 0 else 1.0)
+            # planes it visits (l1 <= (k1 - l1) mod N); the native kernel all
+            # of B; the on-the-fly kernel no table of N^6 size (its gathers
+            # from the compact F-table hit L2)
+            visited = sum(k1 // 2 + 1 + max(0, (k1 + Nf) // 2 - k1) for k1 in range(Nf)) / Nf ** 2
+            frac = {0: visited, 1: 1.0, 2: 0.0}[kind]
+            n2 = 3 * (2 * (Nf - 1 - (Nf - 1) // 2)) ** 2  # largest squared norm (genB's amax)
+            table = {0: nb, 1: nb, 2: (n2 + 1) * (n2 // 4 + 1) * 8 + Nf ** 3 * 16}[kind]
             res[name] = {"evals_per_s": 1.0 / t, "ms_per_eval": t * 1e3,
                          "B_stream_GBs": nb / t / 1e9,
-                         "B_read_GBs": nb * frac / t / 1e9}
+                         "B_read_GBs": nb * frac / t / 1e9,
+                         "table_bytes": table}
         fp64[f"N{Nf}"] = res
         del q64
     peaks, peak_src = measured_peaks()
