@@ -282,9 +282,11 @@ def main():
                     help="calq64: build only the compact tables (genB_compact)")
     ap.add_argument("--probe-reps", type=int, default=2)
     ap.add_argument("--probe-variant", type=int, default=-1,
-                    help="calq32: this kernel variant instead of the autotuned one")
+                    help="calq32: this kernel variant instead of the autotuned one; "
+                         "calq64: this launch shape of the double-float kernel")
     ap.add_argument("--probe-sweep", action="store_true",
-                    help="calq32: time every kernel variant (no chunks and 8 chunks)")
+                    help="calq32: time every kernel variant (no chunks and 8 chunks); "
+                         "calq64: every launch shape of the double-float kernel")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -451,6 +453,7 @@ def main():
     cfg1 = run_config1(edb, data)
     serve = run_serving(edb, args, rank) if args.serve_requests > 0 else None
     uneven = None if args.no_uneven else run_uneven(edb, args, rank)
+    grouped = None if args.no_uneven else run_grouped(edb, args)
 
     line = None
     if rank == 0:
@@ -500,6 +503,7 @@ def main():
         }
         if uneven is not None:
             line["uneven_batch"] = uneven
+            line["grouped_launch"] = grouped
         print(json.dumps(line), flush=True)
     if pg is not None:
         pg.barrier()
@@ -514,7 +518,8 @@ def probe(args):
         table, L = --probe-L), the autotuned variant or --probe-variant;
         --probe-sweep times every variant with 1 and 8 chunks first;
       --probe calq64: FP64 drop-in Q-hat of one BKW solve (index mode
-        --probe-mode).
+        --probe-mode); the double-float kernel in its tuned launch shape or
+        --probe-variant, --probe-sweep times every shape first.
     Prints the per-launch time from CUDA events (not meaningful under ncu)."""
     import ctypes as C
 
@@ -584,6 +589,26 @@ def probe(args):
         def run():
             q.calQ_device(fin, out, stream)
         terms = float(q.info()["terms"])
+        if not args.probe_compact and args.probe_kernel == 0:
+            tuned = q.fp64_shape()
+            if args.probe_sweep:  # every launch shape of the double-float kernel
+                first = None
+                for shp in range(edb.lib.edb_qcalc_fp64_shapes()):
+                    q.fp64_shape(shp)
+                    run()
+                    torch.cuda.synchronize()
+                    first = out.clone() if first is None else first
+                    a0 = torch.cuda.Event(enable_timing=True)
+                    a1 = torch.cuda.Event(enable_timing=True)
+                    a0.record(stream)
+                    for _ in range(args.probe_reps):
+                        run()
+                    a1.record(stream)
+                    torch.cuda.synchronize()
+                    print(f"shape {shp}: {a0.elapsed_time(a1) / args.probe_reps:.3f} ms, bits "
+                          f"{'same' if torch.equal(out, first) else 'DIFFER'}")
+            q.fp64_shape(tuned if args.probe_variant < 0 else args.probe_variant)
+            print(f"double-float kernel shape {q.fp64_shape()} (tuned at genB: {tuned})")
     run()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -692,6 +717,86 @@ def run_uneven(edb, args, rank):
                        "gamma U{0,0.5,1}, SSP3 dt=0.005, U{20..200} steps, fix on, conservative",
            "makespan_s": st["last_done_s"], "hbm_peak_GB": st["hbm_bytes_peak"] / 1e9}
     out.update({k: st[k] for k in SERVE_KEYS})
+    return out
+
+
+def run_grouped(edb, args):
+    """The uneven mix's nine kernel tables (N = 16/24/32 x gamma = 0/0.5/1,
+    L 6/7/8), each with per_N / 3 solves, one Q-hat evaluation each: one
+    grouped launch (a descriptor per table, indexed by CTA; its autotuned
+    variant, and variant 4) against the per-table launches on nine streams
+    and on one stream (variant 4, and each table's autotuned variant).  Tables
+    larger than L2 (2.1 GB at N = 32); CUDA events on the launching stream."""
+    import torch
+    from entropydecreaseboltzmann_gb300 import serving
+
+    S = max(1, args.uneven_per_n // 3)
+    tabs = []
+    for N in (16, 24, 32):
+        for gamma in (0.0, 0.5, 1.0):
+            q = edb.QCalculator(N, int(gamma), gamma=gamma, L=serving.L_OF_N[N], filter=False,
+                                index_mode=edb.INDEX_ALIASED)
+            q.genB()
+            g = torch.Generator(device="cuda").manual_seed(N * 10 + int(2 * gamma))
+            fin = torch.randn(S, N ** 3, dtype=torch.complex64, device="cuda", generator=g)
+            tabs.append([q, S, fin, torch.empty_like(fin)])
+    for t in tabs:
+        t.append(t[0].autotune_batch(S, t[2], t[3]))
+    main = torch.cuda.current_stream()
+    streams = [torch.cuda.Stream() for _ in tabs]
+
+    group = [t[:4] for t in tabs]
+    gvar = edb.QCalculator.autotune_batch_multi(group, stream=main)
+
+    def grouped(var=None):
+        edb.QCalculator.calQ_batch_multi(group, variant=gvar if var is None else var, stream=main)
+
+    def per_stream(var):
+        ev = torch.cuda.Event()
+        ev.record(main)
+        done = []
+        for t, st in zip(tabs, streams):
+            st.wait_event(ev)
+            t[0].calQ_batch_f32_ex(S, t[4] if var is None else var, 1, None, t[2], t[3], stream=st)
+            e = torch.cuda.Event()
+            e.record(st)
+            done.append(e)
+        for e in done:
+            main.wait_event(e)
+
+    def one_stream(var):
+        for t in tabs:
+            t[0].calQ_batch_f32_ex(S, t[4] if var is None else var, 1, None, t[2], t[3],
+                                   stream=main)
+
+    def timed(fn, reps=5):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(main)
+        for _ in range(reps):
+            fn()
+        b.record(main)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    out = {"workload": f"9 tables (N 16/24/32 x gamma 0/0.5/1), {S} solves each, one Q-hat "
+                       "evaluation per solve", "solves": 9 * S,
+           "grouped_ms": timed(grouped), "grouped_variant": gvar,
+           "grouped_variant4_ms": timed(lambda: grouped(4)),
+           "streams_variant4_ms": timed(lambda: per_stream(4)),
+           "streams_autotuned_ms": timed(lambda: per_stream(None)),
+           "one_stream_variant4_ms": timed(lambda: one_stream(4)),
+           "one_stream_autotuned_ms": timed(lambda: one_stream(None)),
+           "autotuned_variants": [t[4] for t in tabs]}
+    # the grouped launch's bits equal the per-table launches' (any variant, one chunk)
+    ref = [t[3].clone() for t in tabs]
+    grouped()
+    torch.cuda.synchronize()
+    out["bit_identical_to_per_table"] = all(torch.equal(r, t[3]) for r, t in zip(ref, tabs))
+    del tabs
+    torch.cuda.synchronize()
     return out
 
 

@@ -113,10 +113,14 @@ def _load():
         "edb_qcalc_calQ_batch_f32_ex": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp,
                                                   _vp]),
         "edb_qcalc_autotune_batch": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _ip]),
+        "edb_qcalc_calQ_batch_multi": (C.c_int, [C.c_int, _vp, _ip, _vp, _vp, C.c_int, _vp]),
+        "edb_qcalc_autotune_batch_multi": (C.c_int, [C.c_int, _vp, _ip, _vp, _vp, _vp, _ip]),
         "edb_qcalc_batch_variants": (C.c_int, []),
         "edb_device_status": (C.c_int, [_ip, C.c_int]),
         "edb_set_wait_limit_ns": (C.c_int, [C.c_longlong]),
         "edb_qcalc_set_fp64_kernel": (C.c_int, [_vp, C.c_int]),
+        "edb_qcalc_fp64_shape": (C.c_int, [_vp, C.c_int, _ip]),
+        "edb_qcalc_fp64_shapes": (C.c_int, []),
         "edb_qcalc_copy_B": (C.c_int, [_vp, C.c_longlong, C.c_longlong, _dp]),
         "edb_qcalc_set_B": (C.c_int, [_vp, _dp]),
         "edb_qcalc_get_info": (C.c_int, [_vp, C.POINTER(QCalcInfo)]),

@@ -131,10 +131,43 @@ class QCalculator:
                                               devptr(d_partial), devptr(d_fin), devptr(d_Q),
                                               stream_ptr(stream)))
 
+    @staticmethod
+    def _multi_args(tables):
+        n = len(tables)
+        return (n, (C.c_void_p * n)(*[t[0]._h for t in tables]),
+                (C.c_int * n)(*[int(t[1]) for t in tables]),
+                (C.c_void_p * n)(*[devptr(t[2]) for t in tables]),
+                (C.c_void_p * n)(*[devptr(t[3]) for t in tables]))
+
+    @staticmethod
+    def calQ_batch_multi(tables, variant=-1, stream=None):
+        """Batched Q-hat of several tables in one launch: tables is a list of
+        (QCalculator, S, d_fin, d_Q), 1 to 16 entries, each handle in ALIASED
+        mode after genB with N % 4 == 0.  variant: 0-4, or -1 for the heaviest
+        table's autotuned one.  Same bits as calQ_batch_f32_ex with one chunk,
+        table by table."""
+        check(lib.edb_qcalc_calQ_batch_multi(*QCalculator._multi_args(tables), int(variant),
+                                             stream_ptr(stream)))
+
+    @staticmethod
+    def autotune_batch_multi(tables, stream=None):
+        """The fastest plain-layout variant for this grouped launch."""
+        v = C.c_int()
+        check(lib.edb_qcalc_autotune_batch_multi(*QCalculator._multi_args(tables),
+                                                 stream_ptr(stream), C.byref(v)))
+        return v.value
+
     def set_fp64_kernel(self, kind):
         """0 = FP64-accurate double-float on the FP32 pipe (default), 1 = native FP64,
         2 = double-float with the pair entries formed on the fly (no N^6 table)."""
         check(lib.edb_qcalc_set_fp64_kernel(self._h, int(kind)))
+
+    def fp64_shape(self, shape=-1):
+        """Launch shape of the double-float FP64 kernel (timed at genB); shape
+        >= 0 overrides it.  Returns the shape in use."""
+        v = C.c_int()
+        check(lib.edb_qcalc_fp64_shape(self._h, int(shape), C.byref(v)))
+        return v.value
 
     def autotune_batch(self, S, d_fin, d_Q, stream=None):
         """Pick the fastest batched-kernel variant for S solves; returns its index."""

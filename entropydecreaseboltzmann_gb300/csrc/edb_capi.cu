@@ -123,7 +123,7 @@ struct edb_qcalc {
   float4 *bs = nullptr;
   int amax = 0;
   int fp64_kernel = EDB_FP64_EMULATED;
-  int c64x_minb = 2;    // register cap of the double-float kernel, tuned at genB
+  int c64x_shape = 0;   // launch shape of the double-float kernel, tuned at genB
   double2 *partial = nullptr;
   double2 *fin = nullptr, *Q = nullptr;  // host-API staging
   int nchunk = 0;
@@ -257,9 +257,9 @@ static edb_status qcalc_alloc_work(edb_qcalc *q) {
   return EDB_OK;
 }
 
-// Times both register caps of the double-float kernel on this table (input:
-// the zeroed staging buffer; the kernel's cost does not depend on the values)
-// and keeps the faster.
+// Times every launch shape (CTA size, register cap) of the double-float
+// kernel on this table (input: the zeroed staging buffer; the kernel's cost
+// does not depend on the values) and keeps the fastest.
 static edb_status qcalc_tune_fp64(edb_qcalc *q) {
   if (!q->B2) return EDB_OK;
   cudaStream_t st = q->st;
@@ -269,13 +269,13 @@ static edb_status qcalc_tune_fp64(edb_qcalc *q) {
   EDB_CUDA(cudaEventCreate(&e0));
   EDB_CUDA(cudaEventCreate(&e1));
   float best = 1e30f;
-  int best_minb = 2;
+  int best_shape = 0;
   edb_status rc = EDB_OK;
-  for (int minb = 2; minb >= 1 && rc == EDB_OK; --minb) {
-    rc = launch_calq64x(q->p, q->B2, q->fdf, q->partial, q->Q, st, minb, qcalc_b2_paired(q));
+  for (int shape = 0; shape < calq64x_shapes() && rc == EDB_OK; ++shape) {
+    rc = launch_calq64x(q->p, q->B2, q->fdf, q->partial, q->Q, st, shape, qcalc_b2_paired(q));
     cudaEventRecord(e0, st);
     for (int r = 0; r < 2 && rc == EDB_OK; ++r)
-      rc = launch_calq64x(q->p, q->B2, q->fdf, q->partial, q->Q, st, minb, qcalc_b2_paired(q));
+      rc = launch_calq64x(q->p, q->B2, q->fdf, q->partial, q->Q, st, shape, qcalc_b2_paired(q));
     cudaEventRecord(e1, st);
     cudaError_t ce = cudaEventSynchronize(e1);
     if (ce != cudaSuccess) {
@@ -286,12 +286,12 @@ static edb_status qcalc_tune_fp64(edb_qcalc *q) {
     cudaEventElapsedTime(&ms, e0, e1);
     if (ms < best) {
       best = ms;
-      best_minb = minb;
+      best_shape = shape;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  q->c64x_minb = best_minb;
+  q->c64x_shape = best_shape;
   if (rc != EDB_OK) return rc;
   return check_device_waits("genB (FP64 kernel timing)");
 }
@@ -501,7 +501,7 @@ static edb_status qcalc_fp64(edb_qcalc *q, const double2 *in, double2 *out, cuda
   }
   if (q->fp64_kernel == EDB_FP64_EMULATED && q->B2) {
     EDB_TRY(launch_split_f(q->p.NQ, in, q->fdf, st));
-    return launch_calq64x(q->p, q->B2, q->fdf, q->partial, out, st, q->c64x_minb,
+    return launch_calq64x(q->p, q->B2, q->fdf, q->partial, out, st, q->c64x_shape,
                           qcalc_b2_paired(q));
   }
   return launch_calq64(q->p, q->B64, in, q->partial, out, st);
@@ -512,6 +512,14 @@ extern "C" edb_status edb_qcalc_set_fp64_kernel(edb_qcalc *q, int kind) {
   if (kind != EDB_FP64_EMULATED && kind != EDB_FP64_NATIVE && kind != EDB_FP64_ONTHEFLY)
     return fail(EDB_EINVAL, "unknown kind");
   q->fp64_kernel = kind;
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_qcalc_fp64_shape(edb_qcalc *q, int shape, int *current) {
+  if (!q) return fail(EDB_EINVAL, "null handle");
+  if (shape >= calq64x_shapes()) return fail(EDB_EINVAL, "unknown launch shape");
+  if (shape >= 0) q->c64x_shape = shape;
+  if (current) *current = q->c64x_shape;
   return EDB_OK;
 }
 
@@ -600,6 +608,7 @@ edb_status qcalc_autotune_split(edb_qcalc *q, int S, const float2 *d_fin, float2
 }  // namespace edb
 
 extern "C" int edb_qcalc_batch_variants(void) { return calq32_variants(); }
+extern "C" int edb_qcalc_fp64_shapes(void) { return calq64x_shapes(); }
 
 extern "C" edb_status edb_qcalc_calQ_batch_f32_ex(edb_qcalc *q, int S, int variant, int chunks,
                                                   void *d_partial, const float *d_fin,
@@ -614,6 +623,91 @@ extern "C" edb_status edb_qcalc_calQ_batch_f32_ex(edb_qcalc *q, int S, int varia
   return launch_calq32_batch(q->d.N, S, q->B32, (const float2 *)d_fin, (float2 *)d_Qout,
                              (cudaStream_t)stream, variant, chunks, (float4 *)d_partial,
                              q->pairs);
+}
+
+// Table entries of a grouped launch (checked), and the variant the auto rule
+// picks: the heaviest table's autotuned variant for its S (a pair variant's
+// plain twin), else 4.
+static edb_status multi_inputs(int ntab, edb_qcalc *const *qs, const int *S,
+                               const float *const *d_fin, float *const *d_Qout, C32MultiIn *in,
+                               int *auto_variant) {
+  if (ntab < 1 || ntab > 16) return fail(EDB_EINVAL, "1 to 16 tables per launch");
+  if (!qs || !S || !d_fin || !d_Qout) return fail(EDB_EINVAL, "null argument");
+  double heaviest = -1.0;
+  *auto_variant = 4;
+  for (int i = 0; i < ntab; ++i) {
+    if (!qs[i] || !d_fin[i] || !d_Qout[i]) return fail(EDB_EINVAL, "null table entry");
+    if (S[i] < 1) return fail(EDB_EINVAL, "S must be positive");
+    if (!qs[i]->B32) return fail(EDB_ENOTREADY, "grouped calQ before genB (ALIASED)");
+    const int N = qs[i]->d.N;
+    if (N % 4) return fail(EDB_EINVAL, "grouped calQ needs N % 4 == 0");
+    in[i] = C32MultiIn{N, S[i], qs[i]->B32, (const float2 *)d_fin[i], (float2 *)d_Qout[i]};
+    const double work = (double)S[i] * std::pow((double)N, 6.0);
+    if (work > heaviest) {
+      heaviest = work;
+      bool tuned = false;
+      const int v = qcalc_c32_variant(qs[i], S[i], &tuned, false);
+      *auto_variant = !tuned ? 4 : (calq32_pair(v) ? v - 5 : v);
+    }
+  }
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_qcalc_calQ_batch_multi(int ntab, edb_qcalc *const *qs, const int *S,
+                                                 const float *const *d_fin,
+                                                 float *const *d_Qout, int variant,
+                                                 void *stream) {
+  C32MultiIn in[16];
+  int v = 4;
+  EDB_TRY(multi_inputs(ntab, qs, S, d_fin, d_Qout, in, &v));
+  if (variant >= 0) v = variant;
+  return launch_calq32_multi(ntab, in, v, (cudaStream_t)stream);
+}
+
+extern "C" edb_status edb_qcalc_autotune_batch_multi(int ntab, edb_qcalc *const *qs,
+                                                     const int *S, const float *const *d_fin,
+                                                     float *const *d_Qout, void *stream,
+                                                     int *chosen) {
+  if (!chosen) return fail(EDB_EINVAL, "null output");
+  C32MultiIn in[16];
+  int v0 = 4;
+  EDB_TRY(multi_inputs(ntab, qs, S, d_fin, d_Qout, in, &v0));
+  const cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t e0, e1;
+  EDB_CUDA(cudaEventCreate(&e0));
+  EDB_CUDA(cudaEventCreate(&e1));
+  int best = -1;
+  float best_ms = 1e30f;
+  edb_status rc = EDB_OK;
+  for (int v = 0; v < calq32_variants() && rc == EDB_OK; ++v) {
+    if (calq32_pair(v)) continue;
+    rc = launch_calq32_multi(ntab, in, v, st);  // warm-up; EINVAL: does not fit
+    if (rc == EDB_EINVAL) {
+      rc = EDB_OK;
+      continue;
+    }
+    if (rc != EDB_OK) break;
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < 2 && rc == EDB_OK; ++r) rc = launch_calq32_multi(ntab, in, v, st);
+    cudaEventRecord(e1, st);
+    const cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(e, "grouped autotune");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != EDB_OK) return rc;
+  if (best < 0) return fail(EDB_EINVAL, "no variant fits these tables");
+  *chosen = best;
+  return EDB_OK;
 }
 
 extern "C" edb_status edb_qcalc_autotune_batch(edb_qcalc *q, int S, const float *d_fin,

@@ -132,10 +132,12 @@ edb_status launch_split_B(long long n, const double *B, float2 *B2, cudaStream_t
 // ALIASED tables: B2 = split of the symmetric pair table (B[l][k] + B[k-l][k]
 // off the planes l1 = m1), read by launch_calq64x with paired = true.
 edb_status launch_split_B_paired(int N, const double *B, float2 *B2, cudaStream_t st);
-// minb selects the register cap (2: 128 registers, 1: up to 255).  paired:
-// B2 is the pair table and only the l1 planes with l1 <= m1 are visited.
+// shape in [0, calq64x_shapes()) selects the CTA size and register cap (timed
+// per table at genB).  paired: B2 is the pair table and only the l1 planes
+// with l1 <= m1 are visited.
+int calq64x_shapes();
 edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const float4 *d_fdf,
-                          double2 *d_partial, double2 *d_Q, cudaStream_t st, int minb,
+                          double2 *d_partial, double2 *d_Q, cudaStream_t st, int shape,
                           bool paired);
 
 // Batched FP32 calQ (ALIASED): S solves, B32 the symmetric pair table in FFTW
@@ -170,6 +172,18 @@ size_t calq32_pair_bytes(int N, int S);
 edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin,
                                float2 *d_Q, cudaStream_t st, int variant, int C = 1,
                                float4 *d_partial = nullptr, float4 *d_pairs = nullptr);
+// One table of a grouped batched launch: S solves (fin / Q, S x N^3 float2)
+// on the FP32 pair table B32 of their (N, gamma, L).
+struct C32MultiIn {
+  int N, S;
+  const float *B32;
+  const float2 *fin;
+  float2 *Q;
+};
+// Q-hat of several tables' solves in one launch (1 to 16 tables, each with
+// N % 4 == 0) with one plain-layout variant (0-4): the per-table results, bit
+// for bit.
+edb_status launch_calq32_multi(int ntab, const C32MultiIn *in, int variant, cudaStream_t st);
 // Reads (and optionally clears) the batched kernel's / the double-float FP64
 // kernel's status word: nonzero when a bounded wait inside it ran out.
 edb_status read_calq32_status(int *status, bool clear);

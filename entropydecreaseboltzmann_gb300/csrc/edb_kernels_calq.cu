@@ -12,6 +12,8 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <cstring>
+#include <vector>
 
 #include "edb_internal.cuh"
 
@@ -806,13 +808,16 @@ __global__ void c32_pairs_kernel(int S, long long NQ, const float2 *__restrict__
 // solve-pair layout (c32_pairs_kernel) and lane w holds solves 2w, 2w+1 of
 // the group; otherwise fin is plain and lane w holds solves w, w+WS.  The
 // autotuner picks the variant per (table, S).
+// The work of one CTA: CTA number lin of a grid of U x GY x GZ = (solve
+// groups x chunks, N, k2 tiles) CTAs over one table (see calq32_kernel).
 template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB, bool PAIR>
-__global__ void __launch_bounds__(MAXT, MINB)
-    calq32_kernel(int N, int S, int K2T, int NST, int NPL, int C, int GB,
-                  const float *__restrict__ B32, const float2 *__restrict__ fin,
-                  float2 *__restrict__ Q, float4 *__restrict__ partial, int tmap,
-                  unsigned long long wait_ns, const __grid_constant__ CUtensorMap tmB,
-                  const __grid_constant__ CUtensorMap tmF) {
+__device__ __forceinline__ void calq32_cta(int N, int S, int K2T, int NST, int NPL, int C, int GB,
+                                           const float *__restrict__ B32,
+                                           const float2 *__restrict__ fin,
+                                           float2 *__restrict__ Q, float4 *__restrict__ partial,
+                                           int tmap, unsigned long long wait_ns,
+                                           const CUtensorMap *tmB, const CUtensorMap *tmF, int U,
+                                           int GY, int GZ, long long lin, int nthr) {
   constexpr int SG = SC * WS;  // solves per group
   extern __shared__ __align__(128) unsigned char smem[];
   const C32Geom g =
@@ -837,19 +842,20 @@ __global__ void __launch_bounds__(MAXT, MINB)
   // CTA -> (unit = solve group x chunk, k1, k2 tile).  Blocks of GB units walk
   // every (k1, tile) before the next block starts, so a block's f-hat stays in
   // L2 while the table streams once per block (the grid is (units, N, tiles)).
-  const int U = gridDim.x, NT = gridDim.y * gridDim.z;
-  const long long lin =
-      blockIdx.x + (long long)U * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
+  const int NT = GY * GZ;
   const int blk = (int)(lin / ((long long)GB * NT));
   const int gsz = min(GB, U - blk * GB);
   const long long off = lin - (long long)blk * GB * NT;
   const int kt = (int)(off / gsz);
   const int unit = blk * GB + (int)(off % gsz);
-  const int k1 = kt % gridDim.y;
-  const int k2_0 = (kt / gridDim.y) * K2T;
+  const int k1 = kt % GY;
+  const int k2_0 = (kt / GY) * K2T;
   const int k2n = min(K2T, N - k2_0);
   const int k2 = k2_0 + k2l;
-  const bool k_ok = (k2l < k2n);
+  // threads past nthr (a grouped launch's block is its largest table's) take
+  // part in the barriers only
+  const bool act = tid < nthr;
+  const bool k_ok = act && (k2l < k2n);
   const int k2c = k_ok ? k2 : k2_0;
   const int k3_0 = r * A;
   const int chunk = unit % C;
@@ -916,7 +922,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
   if (TMA && warp == 0 && nlines > 0) {
     for (int j = 0; j < NST - 1 && j < nlines; ++j) {
       stage_line<true>(g, line_li(j), P0 * N + j, j % NST, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls,
-                       full, tmap, &tmB, &tmF);
+                       full, tmap, tmB, tmF);
       if (lane == 0) ++fills[j % NST];
     }
     stage_plane<true>(g, (k1 - plane_l1(P0) + N) % N, u0, nval, NQ, fin, plb, &pbar[0]);
@@ -967,7 +973,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
         if (j >= 1) mbar_wait(&empty[sn], (uint32_t)(((j - 1) / NST) & 1), to, wait_ns);
         if (!__any_sync(warp_mask(), to)) {
           stage_line<true>(g, line_li(jn), P0 * N + jn, sn, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs,
-                           fls, full, tmap, &tmB, &tmF);
+                           fls, full, tmap, tmB, tmF);
           if (lane == 0) ++fills[sn];
         }
       }
@@ -975,11 +981,12 @@ __global__ void __launch_bounds__(MAXT, MINB)
     } else {
       __syncthreads();  // previous line's readers are done (single buffer)
       stage_line<false>(g, li, P0 * N + j, st, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full,
-                        tmap, &tmB, &tmF);
+                        tmap, tmB, tmF);
       __syncthreads();
     }
 
     // ---- compute line (l1, l2)
+    if (act) {
     const int m2 = (k2c - l2 + N) % N;
     const float *Bt = Bs + (size_t)st * g.BSTG + k2l * N + k3_0;
     const float2 *fl0 = fls + (size_t)st * g.FSTG + (size_t)w * g.FLS;
@@ -1000,6 +1007,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
         compute_line<true, true, A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
       else
         compute_line<false, false, A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
+    }
     }
     if (TMA) {
       // a warp releases the stage only when every lane saw this line's copy
@@ -1106,6 +1114,52 @@ __global__ void __launch_bounds__(MAXT, MINB)
       }
     }
   }
+}
+
+// One table per launch: grid (solve groups x chunks, N, k2 tiles).
+template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB, bool PAIR>
+__global__ void __launch_bounds__(MAXT, MINB)
+    calq32_kernel(int N, int S, int K2T, int NST, int NPL, int C, int GB,
+                  const float *__restrict__ B32, const float2 *__restrict__ fin,
+                  float2 *__restrict__ Q, float4 *__restrict__ partial, int tmap,
+                  unsigned long long wait_ns, const __grid_constant__ CUtensorMap tmB,
+                  const __grid_constant__ CUtensorMap tmF) {
+  const long long lin =
+      blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
+  calq32_cta<TMA, MAXT, HLS, WS, A, MINB, PAIR>(N, S, K2T, NST, NPL, C, GB, B32, fin, Q, partial,
+                                               tmap, wait_ns, &tmB, &tmF, gridDim.x, gridDim.y,
+                                               gridDim.z, lin, (int)blockDim.x);
+}
+
+// Several tables in one launch (uneven N, each table shared by its solves):
+// a descriptor per table, indexed by CTA.  Table t owns the CTAs
+// [begin, begin + U GY GZ) of a 1-D grid and runs them as its own launch
+// would (same tile shape and CTA order, so the same bits); the block is the
+// largest of the tables' (a smaller table leaves its extra threads idle).
+struct C32Table {
+  CUtensorMap tmB, tmF;  // 64-byte aligned
+  const float *B32;
+  const float2 *fin;
+  float2 *Q;
+  long long begin;
+  int N, S, K2T, NST, NPL, GB, U, GY, GZ, tmap, threads;
+};
+constexpr int C32_MULTI_MAX = 16;
+struct C32Multi {
+  C32Table t[C32_MULTI_MAX];
+  int ntab;
+};
+
+template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB, bool PAIR>
+__global__ void __launch_bounds__(MAXT, MINB)
+    calq32_multi_kernel(const __grid_constant__ C32Multi mt, unsigned long long wait_ns) {
+  int t = 0;
+  while (t + 1 < mt.ntab && (long long)blockIdx.x >= mt.t[t + 1].begin) ++t;
+  const C32Table &d = mt.t[t];
+  calq32_cta<TMA, MAXT, HLS, WS, A, MINB, PAIR>(d.N, d.S, d.K2T, d.NST, d.NPL, 1, d.GB, d.B32,
+                                               d.fin, d.Q, nullptr, d.tmap, wait_ns, &d.tmB,
+                                               &d.tmF, d.U, d.GY, d.GZ,
+                                               (long long)blockIdx.x - d.begin, d.threads);
 }
 
 // Chunk reduction: Q = sum over chunks (in order) of hi + lo, in FP64.
@@ -1225,14 +1279,18 @@ static edb_status launch_c32_variant(int v, dim3 grid, int threads, size_t smem,
 #undef EDB_C32
 }
 
-edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin, float2 *d_Q,
-                               cudaStream_t st, int variant, int C, float4 *d_partial,
-                               float4 *d_pairs) {
-  if (variant < 0 || variant >= calq32_variants()) variant = 0;
-  if (C < 1 || C > N) return fail(EDB_EINVAL, "calq32: chunk count must be in [1, N]");
-  if (C > 1 && !d_partial) return fail(EDB_EINVAL, "calq32: chunks need a partial-sum buffer");
-  const C32Variant &vr = kC32Variants[variant];
-  if (vr.pair && !d_pairs) return fail(EDB_EINVAL, "calq32: pair variants need a pair buffer");
+// Tile shape, staging path, tensor maps and pipeline depth of one table's
+// launch (the same for a single-table and a grouped launch).  src: the input
+// the f_l lines and planes are staged from (the solve-pair copy for PAIR).
+struct C32Setup {
+  int K2T, tiles, threads, NST, NPL, GB;
+  bool tma;
+  C32Maps maps;
+  size_t bytes;
+};
+
+static edb_status c32_setup(int N, int S, const C32Variant &vr, int C, const float *d_B32,
+                            const float2 *src, int block_threads, C32Setup *o) {
   const int maxt = vr.maxt, WS = vr.ws, A = vr.a;
   const int SG = SC * WS;
   const int R = (N + A - 1) / A;
@@ -1241,18 +1299,19 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   if (K2T < 1) return fail(EDB_EINVAL, "calq32: N too large for the thread tile");
   const int tiles = (N + K2T - 1) / K2T;
   K2T = (N + tiles - 1) / tiles;
-  const int threads = K2T * R * WS;
-  const int hlt = vr.hls ? threads : 0;
+  o->K2T = K2T;
+  o->tiles = tiles;
+  o->threads = K2T * R * WS;
+  const int bt = block_threads > 0 ? block_threads : o->threads;
+  const int hlt = vr.hls ? bt : 0;
   // TMA bulk copies need 16-byte aligned sources: N % 4 == 0 makes every
   // row/line/plane offset a multiple of 16 bytes; the base pointers are checked
-  const float2 *src = vr.pair ? reinterpret_cast<const float2 *>(d_pairs) : d_fin;
   const int units = vr.pair ? WS : SG, el = vr.pair ? 2 : 1;
-  const bool tma = (N % 4) == 0 && N >= A && ((uintptr_t)d_B32 % 16) == 0 &&
-                   ((uintptr_t)src % 16) == 0;
+  o->tma = (N % 4) == 0 && N >= A && ((uintptr_t)d_B32 % 16) == 0 && ((uintptr_t)src % 16) == 0;
   // line staging by two tensor copies when the f_l box fits (<= 256 floats a
   // row), else by one bulk copy per B row and f_l line
-  C32Maps maps{};
-  if (tma && 2 * c32_geom(N, A, K2T, 1, 1, 0, units, el, true).FLS <= 256 && N <= 256) {
+  o->maps = C32Maps{};
+  if (o->tma && 2 * c32_geom(N, A, K2T, 1, 1, 0, units, el, true).FLS <= 256 && N <= 256) {
     const int FLS = c32_geom(N, A, K2T, 1, 1, 0, units, el, true).FLS;
     const long long NQ = (long long)N * N * N;
     // pair table [k1][visited line][l3][k2][k3]: dims k3, k2, l3, visited line, k1
@@ -1266,35 +1325,55 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
     const cuuint64_t fdim[3] = {(cuuint64_t)N * 2 * el, (cuuint64_t)N * N, (cuuint64_t)nunits};
     const cuuint64_t fstr[2] = {(cuuint64_t)N * 8 * el, (cuuint64_t)NQ * 8 * el};
     const cuuint32_t fbox[3] = {(cuuint32_t)(2 * FLS), 1, (cuuint32_t)units};
-    if (encode_map(&maps.B, 5, d_B32, bdim, bstr, bbox) &&
-        encode_map(&maps.F, 3, src, fdim, fstr, fbox))
-      maps.tmap = 1;
+    if (encode_map(&o->maps.B, 5, d_B32, bdim, bstr, bbox) &&
+        encode_map(&o->maps.F, 3, src, fdim, fstr, fbox))
+      o->maps.tmap = 1;
   }
   // deepest pipeline that fits: two planes with >= 3 stages if possible,
   // else one plane with up to MAX_ST stages (the plain path uses 1 + 1)
   const size_t cap = vr.minb == 2 ? 113 * 1024 : 227 * 1024;
   int NST = 1, NPL = 1;
-  if (tma) {
+  if (o->tma) {
     NST = 0;
     for (int ns = MAX_ST; ns >= 3 && !NST; --ns)
-      if (c32_geom(N, A, K2T, ns, 2, hlt, units, el, maps.tmap).bytes <= cap) {
+      if (c32_geom(N, A, K2T, ns, 2, hlt, units, el, o->maps.tmap).bytes <= cap) {
         NST = ns;
         NPL = 2;
       }
     for (int ns = MAX_ST; ns >= 2 && !NST; --ns)
-      if (c32_geom(N, A, K2T, ns, 1, hlt, units, el, maps.tmap).bytes <= cap) {
+      if (c32_geom(N, A, K2T, ns, 1, hlt, units, el, o->maps.tmap).bytes <= cap) {
         NST = ns;
         NPL = 1;
       }
     if (!NST) return fail(EDB_EINVAL, "calq32: this variant does not fit in shared memory");
   }
-  const C32Geom g = c32_geom(N, A, K2T, NST, NPL, hlt, units, el, maps.tmap);
+  const C32Geom g = c32_geom(N, A, K2T, NST, NPL, hlt, units, el, o->maps.tmap);
   if (g.bytes > cap) return fail(EDB_EINVAL, "calq32: this variant does not fit in shared memory");
-  dim3 grid((unsigned)(((S + SG - 1) / SG) * C), (unsigned)N, (unsigned)tiles);
+  o->NST = NST;
+  o->NPL = NPL;
+  o->bytes = g.bytes;
   // solve-group block of the CTA order: about 32 MB of f-hat kept in L2
+  const unsigned U = (unsigned)(((S + SG - 1) / SG) * C);
   const long long group_bytes = (long long)SG * N * N * N * (long long)sizeof(float2);
   int GB = (int)std::max<long long>(1, (32LL << 20) / group_bytes) * C;
-  if (GB > (int)grid.x) GB = (int)grid.x;
+  if (GB > (int)U) GB = (int)U;
+  o->GB = GB;
+  return EDB_OK;
+}
+
+edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin, float2 *d_Q,
+                               cudaStream_t st, int variant, int C, float4 *d_partial,
+                               float4 *d_pairs) {
+  if (variant < 0 || variant >= calq32_variants()) variant = 0;
+  if (C < 1 || C > N) return fail(EDB_EINVAL, "calq32: chunk count must be in [1, N]");
+  if (C > 1 && !d_partial) return fail(EDB_EINVAL, "calq32: chunks need a partial-sum buffer");
+  const C32Variant &vr = kC32Variants[variant];
+  if (vr.pair && !d_pairs) return fail(EDB_EINVAL, "calq32: pair variants need a pair buffer");
+  const int SG = SC * vr.ws;
+  const float2 *src = vr.pair ? reinterpret_cast<const float2 *>(d_pairs) : d_fin;
+  C32Setup su;
+  EDB_TRY(c32_setup(N, S, vr, C, d_B32, src, 0, &su));
+  dim3 grid((unsigned)(((S + SG - 1) / SG) * C), (unsigned)N, (unsigned)su.tiles);
   if (vr.pair) {
     const long long n = (long long)((S + 1) / 2) * N * N * N;
     const long long blocks = std::min<long long>((n + 255) / 256, 16LL * device_sm_count());
@@ -1302,16 +1381,94 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
     EDB_LAUNCHED();
   }
   edb_status rc =
-      tma ? launch_c32_variant<true>(variant, grid, threads, g.bytes, N, S, K2T, NST, NPL, C, GB,
-                                     d_B32, src, d_Q, d_partial, maps, st)
-          : launch_c32_variant<false>(variant, grid, threads, g.bytes, N, S, K2T, NST, NPL, C, GB,
-                                      d_B32, src, d_Q, d_partial, maps, st);
+      su.tma ? launch_c32_variant<true>(variant, grid, su.threads, su.bytes, N, S, su.K2T, su.NST,
+                                        su.NPL, C, su.GB, d_B32, src, d_Q, d_partial, su.maps, st)
+             : launch_c32_variant<false>(variant, grid, su.threads, su.bytes, N, S, su.K2T,
+                                         su.NST, su.NPL, C, su.GB, d_B32, src, d_Q, d_partial,
+                                         su.maps, st);
   if (rc != EDB_OK || C == 1) return rc;
   const long long n = (long long)S * N * N * N;
   const long long blocks = std::min<long long>((n + 255) / 256, 16LL * device_sm_count());
   calq32_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(n, C, d_partial, d_Q);
   EDB_LAUNCHED();
   return EDB_OK;
+}
+
+template <int V>
+static edb_status launch_c32_multi_v(const C32Multi &mt, unsigned blocks, int block, size_t smem,
+                                     cudaStream_t st) {
+  constexpr C32Variant vr = kC32Variants[V];
+  auto kern = calq32_multi_kernel<true, vr.maxt, vr.hls, vr.ws, vr.a, vr.minb, false>;
+  static const cudaError_t configured = cudaFuncSetAttribute(
+      kern, cudaFuncAttributeMaxDynamicSharedMemorySize, vr.minb == 2 ? 113 * 1024 : 227 * 1024);
+  if (configured != cudaSuccess) return cuda_fail(configured, "cudaFuncSetAttribute(calq32 multi)");
+  kern<<<blocks, block, smem, st>>>(mt, wait_limit_ns());
+  EDB_LAUNCHED();
+  return EDB_OK;
+}
+
+// Grouped launch: one plain-layout variant (0-4) for every table, tensor-copy
+// staging required; tables ordered by descending N (their CTAs are the
+// longest) in one 1-D grid, each table's CTAs in its own launch's order.
+edb_status launch_calq32_multi(int ntab, const C32MultiIn *in, int variant, cudaStream_t st) {
+  if (ntab < 1 || ntab > C32_MULTI_MAX)
+    return fail(EDB_EINVAL, "calq32 multi: 1 to 16 tables per launch");
+  if (variant < 0 || variant >= calq32_variants() || kC32Variants[variant].pair)
+    return fail(EDB_EINVAL, "calq32 multi: a plain-layout variant (0-4)");
+  const C32Variant &vr = kC32Variants[variant];
+  const int SG = SC * vr.ws;
+  std::vector<int> order(ntab);
+  for (int i = 0; i < ntab; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return in[a].N > in[b].N; });
+  // the block is the largest table's; every table's shared memory and
+  // pipeline depth is chosen for that block
+  int block = 0;
+  for (int i = 0; i < ntab; ++i) {
+    if (in[i].S < 1 || !in[i].B32 || !in[i].fin || !in[i].Q)
+      return fail(EDB_EINVAL, "calq32 multi: bad table entry");
+    C32Setup su;
+    EDB_TRY(c32_setup(in[i].N, in[i].S, vr, 1, in[i].B32, in[i].fin, 0, &su));
+    block = std::max(block, su.threads);
+  }
+  C32Multi mt;
+  memset(&mt, 0, sizeof(mt));
+  mt.ntab = ntab;
+  long long begin = 0;
+  size_t smem = 0;
+  for (int j = 0; j < ntab; ++j) {
+    const C32MultiIn &e = in[order[j]];
+    C32Setup su;
+    EDB_TRY(c32_setup(e.N, e.S, vr, 1, e.B32, e.fin, block, &su));
+    if (!su.tma || !su.maps.tmap)
+      return fail(EDB_EINVAL, "calq32 multi: every table needs the tensor-copy path (N % 4 == 0)");
+    C32Table &d = mt.t[j];
+    d.tmB = su.maps.B;
+    d.tmF = su.maps.F;
+    d.B32 = e.B32;
+    d.fin = e.fin;
+    d.Q = e.Q;
+    d.begin = begin;
+    d.N = e.N;
+    d.S = e.S;
+    d.K2T = su.K2T;
+    d.NST = su.NST;
+    d.NPL = su.NPL;
+    d.GB = su.GB;
+    d.U = (e.S + SG - 1) / SG;
+    d.GY = e.N;
+    d.GZ = su.tiles;
+    d.tmap = 1;
+    d.threads = su.threads;
+    begin += (long long)d.U * d.GY * d.GZ;
+    smem = std::max(smem, su.bytes);
+  }
+  switch (variant) {
+    case 0: return launch_c32_multi_v<0>(mt, (unsigned)begin, block, smem, st);
+    case 1: return launch_c32_multi_v<1>(mt, (unsigned)begin, block, smem, st);
+    case 2: return launch_c32_multi_v<2>(mt, (unsigned)begin, block, smem, st);
+    case 3: return launch_c32_multi_v<3>(mt, (unsigned)begin, block, smem, st);
+    default: return launch_c32_multi_v<4>(mt, (unsigned)begin, block, smem, st);
+  }
 }
 
 edb_status read_calq32_status(int *status, bool clear) {

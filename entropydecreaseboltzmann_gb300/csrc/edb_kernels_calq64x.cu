@@ -157,11 +157,12 @@ __global__ void b2_pair_split_kernel(int N, const double *__restrict__ B, float2
 
 // TMA: per-warp bulk-copy ring for B (requires contiguous, aligned warp
 // segments; see the launcher).  Otherwise __ldg one row ahead.
-// MINB: minimum resident CTAs per SM the register allocation must allow
-// (2: at most 128 registers per thread; 1: up to 255).  Chosen per shape by
-// timing both (edb_qcalc_genB runs the comparison once per table).
-template <bool TMA, int MINB>
-__global__ void __launch_bounds__(256, MINB)
+// MAXT, MINB: CTA size bound and minimum resident CTAs per SM the register
+// allocation must allow (see kC64xShapes).  The kernel is bound by the latency
+// of its dependent double-float chains, so resident warps matter: chosen per
+// table by timing every shape (edb_qcalc_genB runs the comparison once).
+template <bool TMA, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
     calq64x_kernel(QParams p, int J2T, int LC, int paired, const float2 *__restrict__ B2,
                    const float4 *__restrict__ fdf, double2 *__restrict__ partial,
                    unsigned long long wait_ns) {
@@ -408,9 +409,29 @@ struct C64xPlan {
   size_t smem;
 };
 
+// Launch shapes (CTA size bound, CTAs per SM the registers must allow):
+//   0: 256 threads, 2 CTAs (<= 128 registers)   1: 256, 1 (<= 255)
+//   2: 128 threads, 3 CTAs (<= 168)            3: 128, 4 (<= 128)
+//   4: 192 threads, 2 CTAs (<= 168)
+struct C64xShape {
+  int maxt, minb;
+};
+constexpr C64xShape kC64xShapes[] = {{256, 2}, {256, 1}, {128, 3}, {128, 4}, {192, 2}};
+constexpr int kC64xNShapes = (int)(sizeof(kC64xShapes) / sizeof(kC64xShapes[0]));
+
+template <bool TMA, int S>
+static const void *c64x_fn_s() {
+  return (const void *)calq64x_kernel<TMA, kC64xShapes[S].maxt, kC64xShapes[S].minb>;
+}
 template <bool TMA>
-static const void *c64x_fn(int minb) {
-  return minb == 2 ? (const void *)calq64x_kernel<TMA, 2> : (const void *)calq64x_kernel<TMA, 1>;
+static const void *c64x_fn(int shape) {
+  switch (shape) {
+    case 0: return c64x_fn_s<TMA, 0>();
+    case 1: return c64x_fn_s<TMA, 1>();
+    case 2: return c64x_fn_s<TMA, 2>();
+    case 3: return c64x_fn_s<TMA, 3>();
+    default: return c64x_fn_s<TMA, 4>();
+  }
 }
 
 static size_t c64x_smem(int N, int threads, bool tma) {
@@ -431,27 +452,27 @@ static int c64x_lines(const QParams &p, bool paired) {
   return m * p.N;
 }
 
-static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int minb, bool paired);
-static C64xPlan c64x_plan(const QParams &p, bool aligned, int minb, bool paired) {
+static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int shape, bool paired);
+static C64xPlan c64x_plan(const QParams &p, bool aligned, int shape, bool paired) {
   static std::mutex mu;
   static std::map<long long, C64xPlan> cache;
   int dev = 0;
   cudaGetDevice(&dev);
   const long long key =
-      (((((long long)dev * 128 + p.N) * 4 + p.mode) * 2 + (aligned ? 1 : 0)) * 4 + minb) * 2 +
+      (((((long long)dev * 128 + p.N) * 4 + p.mode) * 2 + (aligned ? 1 : 0)) * 8 + shape) * 2 +
       (paired ? 1 : 0);
   std::lock_guard<std::mutex> lock(mu);
   auto it = cache.find(key);
   if (it != cache.end()) return it->second;
-  C64xPlan pl = c64x_plan_compute(p, aligned, minb, paired);
+  C64xPlan pl = c64x_plan_compute(p, aligned, shape, paired);
   cache[key] = pl;
   return pl;
 }
 
-static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int minb, bool paired) {
+static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int shape, bool paired) {
   C64xPlan pl;
   const int R4 = (p.P + RUN - 1) / RUN;
-  int J2T = 256 / R4;
+  int J2T = std::max(1, kC64xShapes[shape].maxt / R4);
   if (J2T > p.P) J2T = p.P;
   const int tiles = (p.P + J2T - 1) / J2T;
   J2T = (p.P + tiles - 1) / tiles;
@@ -461,7 +482,7 @@ static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int minb, bool
   pl.tma = aligned && (p.P % RUN) == 0 && (p.P % J2T) == 0;
   pl.smem = c64x_smem(p.N, pl.threads, pl.tma);
   int occ = 1;
-  const void *fn = pl.tma ? c64x_fn<true>(minb) : c64x_fn<false>(minb);
+  const void *fn = pl.tma ? c64x_fn<true>(shape) : c64x_fn<false>(shape);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, pl.threads, pl.smem);
   if (occ < 1) occ = 1;
@@ -494,10 +515,10 @@ static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int minb, bool
 int calq64x_nchunk(const QParams &p, int *J2T_out) {
   // upper bound over the variants, used to size the partial-sum buffer
   int n = 1;
-  for (int minb = 1; minb <= 2; ++minb)
+  for (int shape = 0; shape < kC64xNShapes; ++shape)
     for (int al = 0; al <= 1; ++al)
       for (int pa = 0; pa <= 1; ++pa) {
-        const C64xPlan pl = c64x_plan(p, al != 0, minb, pa != 0);
+        const C64xPlan pl = c64x_plan(p, al != 0, shape, pa != 0);
         if (J2T_out) *J2T_out = pl.J2T;
         if (pl.nch > n) n = pl.nch;
       }
@@ -523,30 +544,42 @@ edb_status launch_split_B_paired(int N, const double *B, float2 *B2, cudaStream_
   return EDB_OK;
 }
 
+int calq64x_shapes() { return kC64xNShapes; }
+
+template <bool TMA, int S>
+static void c64x_launch_s(dim3 grid, const C64xPlan &pl, const QParams &p, bool paired,
+                          const float2 *d_B2, const float4 *d_fdf, double2 *d_partial,
+                          cudaStream_t st) {
+  calq64x_kernel<TMA, kC64xShapes[S].maxt, kC64xShapes[S].minb>
+      <<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf, d_partial,
+                                          wait_limit_ns());
+}
+template <bool TMA>
+static void c64x_launch(int shape, dim3 grid, const C64xPlan &pl, const QParams &p, bool paired,
+                        const float2 *d_B2, const float4 *d_fdf, double2 *d_partial,
+                        cudaStream_t st) {
+  switch (shape) {
+    case 0: c64x_launch_s<TMA, 0>(grid, pl, p, paired, d_B2, d_fdf, d_partial, st); break;
+    case 1: c64x_launch_s<TMA, 1>(grid, pl, p, paired, d_B2, d_fdf, d_partial, st); break;
+    case 2: c64x_launch_s<TMA, 2>(grid, pl, p, paired, d_B2, d_fdf, d_partial, st); break;
+    case 3: c64x_launch_s<TMA, 3>(grid, pl, p, paired, d_B2, d_fdf, d_partial, st); break;
+    default: c64x_launch_s<TMA, 4>(grid, pl, p, paired, d_B2, d_fdf, d_partial, st); break;
+  }
+}
+
 edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const float4 *d_fdf,
-                          double2 *d_partial, double2 *d_Q, cudaStream_t st, int minb,
+                          double2 *d_partial, double2 *d_Q, cudaStream_t st, int shape,
                           bool paired) {
-  if (minb != 1) minb = 2;
+  if (shape < 0 || shape >= kC64xNShapes) shape = 0;
   if (paired && (p.P != p.N || (p.sM % p.N) != 0 || (p.sL % p.N) != p.N - p.n))
     return fail(EDB_EINVAL, "calq64x: pairs need the aliased index shifts");
   const bool aligned = ((uintptr_t)d_B2 % 16) == 0;
-  const C64xPlan pl = c64x_plan(p, aligned, minb, paired);
+  const C64xPlan pl = c64x_plan(p, aligned, shape, paired);
   dim3 grid((unsigned)p.P, (unsigned)pl.tiles, (unsigned)pl.nch);
-  if (pl.tma) {
-    if (minb == 2)
-      calq64x_kernel<true, 2><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf,
-                                                                 d_partial, wait_limit_ns());
-    else
-      calq64x_kernel<true, 1><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf,
-                                                                 d_partial, wait_limit_ns());
-  } else {
-    if (minb == 2)
-      calq64x_kernel<false, 2><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf,
-                                                                  d_partial, wait_limit_ns());
-    else
-      calq64x_kernel<false, 1><<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf,
-                                                                  d_partial, wait_limit_ns());
-  }
+  if (pl.tma)
+    c64x_launch<true>(shape, grid, pl, p, paired, d_B2, d_fdf, d_partial, st);
+  else
+    c64x_launch<false>(shape, grid, pl, p, paired, d_B2, d_fdf, d_partial, st);
   EDB_LAUNCHED();
   return launch_calq64_reduce(p, pl.nch, d_partial, d_Q, st);
 }

@@ -180,6 +180,27 @@ int edb_qcalc_batch_variants(void);
 edb_status edb_calQ_fp64_noalloc(int N, int index_mode, const double *d_B, const double *d_fin,
                                  double *d_Qout, void *stream);
 
+/* Batched Q-hat for several tables in ONE launch (no reference counterpart):
+ * table i is handle qs[i] (ALIASED mode, genB done, N % 4 == 0) with S[i]
+ * solves in d_fin[i] / d_Qout[i] (device, layout as
+ * edb_qcalc_calQ_batch_f32_device).  1 to 16 tables.  Each CTA reads its
+ * table's descriptor (N, tile shape, tensor maps, buffers) by its index, so
+ * one launch fills the GPU with a mix of tables that would each leave it
+ * partly idle.  variant: a plain-layout variant 0-4 of
+ * edb_qcalc_calQ_batch_f32_ex for every table, or -1 for the one the
+ * heaviest table (S x N^6) was autotuned to (4 if untuned).  Results equal
+ * edb_qcalc_calQ_batch_f32_ex(qs[i], S[i], any variant, 1, ...) bit for bit. */
+edb_status edb_qcalc_calQ_batch_multi(int ntab, edb_qcalc *const *qs, const int *S,
+                                      const float *const *d_fin, float *const *d_Qout,
+                                      int variant, void *stream);
+
+/* Times the grouped launch with each plain-layout variant on the caller's
+ * buffers (one warm-up and two timed launches each, CUDA events on `stream`)
+ * and returns the fastest in *chosen, for edb_qcalc_calQ_batch_multi. */
+edb_status edb_qcalc_autotune_batch_multi(int ntab, edb_qcalc *const *qs, const int *S,
+                                          const float *const *d_fin, float *const *d_Qout,
+                                          void *stream, int *chosen);
+
 /* Autotuner of the batched kernel (no reference counterpart): times each
  * launch variant (CTA size / k2-tile shape) on the caller's buffers and keeps
  * the fastest for S's size class; later batched calls on this handle use it.
@@ -218,6 +239,15 @@ edb_status edb_set_wait_limit_ns(long long ns);
  * ALIASED mode or odd N).  Used automatically after edb_qcalc_genB_compact. */
 #define EDB_FP64_ONTHEFLY 2
 edb_status edb_qcalc_set_fp64_kernel(edb_qcalc *q, int kind);
+
+/* Launch shape (CTA size and register cap) of the double-float kernel
+ * (EDB_FP64_EMULATED), no reference counterpart: genB times every shape on the
+ * table and keeps the fastest.  shape >= 0 overrides that choice (the results
+ * do not depend on it), -1 leaves it; *current (may be NULL) receives the shape
+ * in use. */
+edb_status edb_qcalc_fp64_shape(edb_qcalc *q, int shape, int *current);
+/* Number of launch shapes of the double-float kernel. */
+int edb_qcalc_fp64_shapes(void);
 
 /* genB without the N^6 table (QCalculator.h:158-229 restated per term): builds
  * only what the on-the-fly FP64 kernel reads, the F-table T(a, b) times the

@@ -305,6 +305,7 @@ def test_fp64_emulated_kernel_matches_native_and_oracle(edb, oracle, N, mode):
     f_int = rng.integers(0, 10, N ** 3) + 1j * rng.integers(0, 10, N ** 3)
     Bo = oracle.genB(N, 0.0, 7.0, mode == INDEX_REFERENCE, mode) if N <= 17 else None
     modes = rng.choice(N ** 3, 128, replace=False)
+    tuned = q.fp64_shape()
     for fin in (f_int, f_bkw):
         q.set_fp64_kernel(0)
         Qe = q.calQ(None, fin)
@@ -319,6 +320,19 @@ def test_fp64_emulated_kernel_matches_native_and_oracle(edb, oracle, N, mode):
             Qd = oracle.direct_modes(N, fin, modes, gamma=0.0, R=7.0, filter=False)
             assert rel_l2(Qe[modes], Qd) <= 1e-12
             assert rel_l2(Qn[modes], Qd) <= 1e-12
+        # every launch shape of the double-float kernel (CTA size, register
+        # cap; the l-line chunking follows the shape) meets the same bound
+        q.set_fp64_kernel(0)
+        for shp in range(edb.lib.edb_qcalc_fp64_shapes()):
+            q.fp64_shape(shp)
+            Qs = q.calQ(None, fin)
+            if Bo is not None:
+                assert rel_l2(Qs, Qo) <= 1e-12, shp
+            else:
+                assert rel_l2(Qs[modes], Qd) <= 1e-12, shp
+        q.fp64_shape(tuned)
+    with pytest.raises(edb.EdbError):
+        q.fp64_shape(edb.lib.edb_qcalc_fp64_shapes())
 
 
 def test_funF_and_filtering_on_device_match_reference_golden(edb, golden):
