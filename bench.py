@@ -109,7 +109,7 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
+        sm, smax, pw, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             p = [x.strip() for x in ln.split(",")]
@@ -120,12 +120,17 @@ class ClockSampler:
                 smax.append(float(p[1]))
             except ValueError:
                 continue
+            try:
+                pw.append(float(p[2]))
+            except ValueError:
+                pass
             for nm, v in zip(names, p[4:8]):
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": float(max(smax)) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w": float(np.median(pw)) if pw else None}
 
 
 def measured_peaks():
@@ -380,12 +385,15 @@ def main():
     _ = bs.read(real=True)
     torch.cuda.synchronize()
     e2e_steps = args.steps
+    e2e_clocks = ClockSampler(local)
+    e2e_clocks.start()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         bs.load(h_in.numpy())
         bs.step(1)
         bs.read(real=True, out=h_out.numpy())
     e2e_s = time.perf_counter() - t0
+    e2e_clk = e2e_clocks.stop()
     e2e_value = evals_per_step * e2e_steps / e2e_s
     h2d = S * NQ * 8
     d2h = S * NQ * 8
@@ -470,7 +478,8 @@ def main():
                        "parallelism": f"replicas x{ws}"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
-                    "path": "edb_batch_load (pinned host) + edb_batch_step + edb_batch_read"},
+                    "path": "edb_batch_load (pinned host) + edb_batch_step + edb_batch_read",
+                    "clocks": e2e_clk},
             "gpu_launches": int(launches),
             "clocks": clk,
             "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf,

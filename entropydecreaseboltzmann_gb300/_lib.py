@@ -149,6 +149,7 @@ def _load():
         "edb_batch_step": (C.c_int, [_vp, C.c_int, _vp]),
         "edb_batch_read": (C.c_int, [_vp, _dp, _dp]),
         "edb_batch_read_device": (C.c_int, [_vp, _vp, _vp]),
+        "edb_batch_entropy": (C.c_int, [_vp, _dp, _dp]),
         "edb_cells_transport_x_device": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double,
                                                    C.c_double, _vp, _vp, _vp]),
         "edb_batch_moments": (C.c_int, [_vp, _dp, _dp]),

@@ -465,7 +465,10 @@ class BatchSolver:
 
     def read(self, real=True, fhat=False, out=None):
         """Real-space f (S x N^3) and/or Fhat.  out: a C-contiguous float64 array of
-        S x N^3 to receive f directly (e.g. pinned host memory), instead of a new one."""
+        S x N^3 to receive f directly (e.g. pinned host memory), instead of a new one.
+        With fix_entropy on, f after a step is the step's output after the fix
+        rule (the reference's F), which differs from ifft(Fhat) where the fix
+        acted."""
         if real and out is not None:
             if out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"] or out.size != self.S * self.NQ:
                 raise ValueError("out must be a contiguous float64 array of S x N^3")
@@ -485,6 +488,14 @@ class BatchSolver:
     def read_device(self, d_F_real, stream=None):
         """Real-space f (S x N^3 float64) into a device buffer (torch tensor or address)."""
         check(lib.edb_batch_read_device(self._h, devptr(d_F_real), stream_ptr(stream)))
+
+    def entropy(self):
+        """(raw, fixed): each solve's entropy after its last step, before and
+        after the fix rule (NaN before the first step)."""
+        raw = np.empty(self.S)
+        fixed = np.empty(self.S)
+        check(lib.edb_batch_entropy(self._h, dptr(raw), dptr(fixed)))
+        return raw, fixed
 
     def moments(self):
         m = np.empty(self.S * 5)

@@ -1240,6 +1240,11 @@ struct edb_batch {
   cudaGraphExec_t exec = nullptr;
   cudaStream_t exec_stream = nullptr;
   int launches_per_step = 0;
+  // F holds the real-space output of the current state: the loaded data, the
+  // last step's F after the fix rule (the step computes it when the fix is
+  // on), or a transform made by a reader.  The reference's output after a
+  // step is that F, which its fix rewrites without touching F-hat.
+  bool f_cur = false;
   // host transfers of load/read in cube chunks on their own stream, so the
   // copy of one chunk overlaps the transforms of the next
   cudaStream_t cst = nullptr;
@@ -1344,6 +1349,9 @@ static edb_status batch_init_state(edb_batch *b, cudaStream_t st, bool transform
   std::vector<EfixState> init((size_t)b->d.S, EfixState{1.0, 0, 0, 1.0, 0, 0});
   EDB_CUDA(cudaMemcpyAsync(b->state, init.data(), sizeof(EfixState) * b->d.S,
                            cudaMemcpyHostToDevice, st));
+  // no step yet: the last-step entropies read as NaN (all-ones bytes)
+  EDB_CUDA(cudaMemsetAsync(b->tr_raw, 0xff, sizeof(double) * b->d.S, st));
+  EDB_CUDA(cudaMemsetAsync(b->tr_fixed, 0xff, sizeof(double) * b->d.S, st));
   if (b->d.conserve) {  // start the entropy rule from the initial entropy
     EDB_TRY(launch_calentropy(b->d.N, b->d.S, b->d.R, b->F, b->H, st));
     EDB_TRY(launch_state_from_entropy(b->d.S, b->H, b->state, st));
@@ -1382,7 +1390,9 @@ extern "C" edb_status edb_batch_load(edb_batch *b, const double *F0_real) {
     EDB_TRY(launch_dft3d(b->d.N, c1 - c0, b->F + c0 * NQ, b->Fhat + c0 * NQ, nullptr, 0, 0,
                          b->st));
   }
-  return batch_init_state(b, b->st, true);
+  EDB_TRY(batch_init_state(b, b->st, true));
+  b->f_cur = true;  // F holds the loaded data
+  return EDB_OK;
 }
 
 // With a NULL stream the device-pointer calls run on the batch's own stream,
@@ -1399,7 +1409,9 @@ extern "C" edb_status edb_batch_load_device(edb_batch *b, const double *d_F0_rea
   if (!stream) EDB_TRY(batch_join_default(b));
   cudaStream_t st = stream ? (cudaStream_t)stream : b->st;
   EDB_TRY(launch_real_to_complex(b->n, d_F0_real, b->F, st));
-  return batch_init_state(b, st);
+  EDB_TRY(batch_init_state(b, st));
+  b->f_cur = true;
+  return EDB_OK;
 }
 
 // One step for every solve: Q-hat stages on the FP32 copy of each stage
@@ -1452,7 +1464,7 @@ static edb_status batch_step_record(edb_batch *b, cudaStream_t st) {
     if (b->d.fix_entropy) {
       EDB_TRY(launch_dft3d(N, S, Fh, b->F, nullptr, 1, 0, st));
       EDB_TRY(launch_step_entropy_conserve(N, S, b->d.R, b->F, b->state, 1.0e-10, 2, b->tr_raw,
-                                           b->tr_fixed, 1, st));
+                                           b->tr_fixed, 1, st, true));
       EDB_TRY(launch_dft3d(N, S, b->F, F[0], nullptr, 0, 0, st));
       EDB_TRY(launch_masked_copy(b->NQ, S, b->state, F[0], Fh, st));
     }
@@ -1460,7 +1472,7 @@ static edb_status batch_step_record(edb_batch *b, cudaStream_t st) {
   } else if (b->d.fix_entropy) {
     EDB_TRY(launch_dft3d(N, S, Fh, b->F, nullptr, 1, 0, st));
     EDB_TRY(launch_step_entropy(N, S, b->d.R, b->F, b->state, 1.0e-10, 2, b->tr_raw, b->tr_fixed,
-                                1, st));
+                                1, st, true));
   }
   return EDB_OK;
 }
@@ -1490,6 +1502,7 @@ extern "C" edb_status edb_batch_step(edb_batch *b, int nsteps, void *stream) {
     EDB_CUDA(cudaGraphLaunch(b->exec, st));
     count_launch(b->launches_per_step);
   }
+  if (nsteps > 0) b->f_cur = b->d.fix_entropy != 0;
   if (!stream) {
     EDB_CUDA(cudaStreamSynchronize(st));
     return check_device_waits("batch step");
@@ -1503,15 +1516,18 @@ extern "C" edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat)
   EDB_CUDA(cudaStreamSynchronize(st));
   if (Fhat)
     EDB_CUDA(cudaMemcpyAsync(Fhat, b->Fhat, sizeof(double2) * b->n, cudaMemcpyDeviceToHost, st));
-  if (F_real) {  // inverse transform, real parts packed on the device, per
-                 // chunk: chunk i copies out while chunk i+1 transforms
+  if (F_real) {  // inverse transform (unless F is current), real parts packed
+                 // on the device, per chunk: chunk i copies out while chunk i+1
+                 // transforms
     double *stage = batch_staging(b);
     const long long NQ = b->NQ;
     for (int i = 0; i < BATCH_XFER_CHUNKS; ++i) {
       int c0, c1;
       batch_chunk(b, i, &c0, &c1);
       if (c1 <= c0) break;
-      EDB_TRY(launch_dft3d(b->d.N, c1 - c0, b->Fhat + c0 * NQ, b->F + c0 * NQ, nullptr, 1, 0, st));
+      if (!b->f_cur)
+        EDB_TRY(
+            launch_dft3d(b->d.N, c1 - c0, b->Fhat + c0 * NQ, b->F + c0 * NQ, nullptr, 1, 0, st));
       EDB_TRY(launch_complex_to_real((c1 - c0) * NQ, b->F + c0 * NQ, stage + c0 * NQ, st));
       EDB_CUDA(cudaEventRecord(b->xev[i], st));
       EDB_CUDA(cudaStreamWaitEvent(b->cst, b->xev[i], 0));
@@ -1519,6 +1535,7 @@ extern "C" edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat)
                                cudaMemcpyDeviceToHost, b->cst));
     }
     EDB_CUDA(cudaStreamSynchronize(b->cst));
+    b->f_cur = true;
   }
   EDB_CUDA(cudaStreamSynchronize(st));
   return EDB_OK;
@@ -1528,8 +1545,8 @@ extern "C" edb_status edb_batch_read_device(edb_batch *b, double *d_F_real, void
   if (!b || !d_F_real) return fail(EDB_EINVAL, "null argument");
   if (!stream) EDB_TRY(batch_join_default(b));
   cudaStream_t st = stream ? (cudaStream_t)stream : b->st;
-  // F is scratch between steps (the step graph rewrites it when the fix runs)
-  EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->Fhat, b->F, nullptr, 1, 0, st));
+  if (!b->f_cur) EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->Fhat, b->F, nullptr, 1, 0, st));
+  b->f_cur = true;
   EDB_TRY(launch_complex_to_real(b->n, b->F, d_F_real, st));
   if (!stream) EDB_CUDA(cudaStreamSynchronize(st));
   return EDB_OK;
@@ -1538,7 +1555,8 @@ extern "C" edb_status edb_batch_read_device(edb_batch *b, double *d_F_real, void
 extern "C" edb_status edb_batch_moments(edb_batch *b, double *moments, double *entropy) {
   if (!b) return fail(EDB_EINVAL, "null handle");
   cudaStream_t st = b->st;
-  EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->Fhat, b->F, nullptr, 1, 0, st));
+  if (!b->f_cur) EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->Fhat, b->F, nullptr, 1, 0, st));
+  b->f_cur = true;
   EDB_TRY(launch_moments(b->d.N, b->d.S, b->d.R, b->F, b->mom, st));
   EDB_TRY(launch_calentropy(b->d.N, b->d.S, b->d.R, b->F, b->H, st));
   if (moments)
@@ -1546,6 +1564,18 @@ extern "C" edb_status edb_batch_moments(edb_batch *b, double *moments, double *e
                              st));
   if (entropy)
     EDB_CUDA(cudaMemcpyAsync(entropy, b->H, sizeof(double) * b->d.S, cudaMemcpyDeviceToHost, st));
+  EDB_CUDA(cudaStreamSynchronize(st));
+  return EDB_OK;
+}
+
+extern "C" edb_status edb_batch_entropy(edb_batch *b, double *raw, double *fixed) {
+  if (!b || (!raw && !fixed)) return fail(EDB_EINVAL, "null argument");
+  cudaStream_t st = b->st;
+  if (raw)
+    EDB_CUDA(cudaMemcpyAsync(raw, b->tr_raw, sizeof(double) * b->d.S, cudaMemcpyDeviceToHost, st));
+  if (fixed)
+    EDB_CUDA(
+        cudaMemcpyAsync(fixed, b->tr_fixed, sizeof(double) * b->d.S, cudaMemcpyDeviceToHost, st));
   EDB_CUDA(cudaStreamSynchronize(st));
   return EDB_OK;
 }

@@ -211,10 +211,13 @@ edb_status launch_calentropy(int N, int batch, double R, const double2 *d_F, dou
                              cudaStream_t st);
 // The integrator's post-step rule (compute H, fix on entropy rise, record
 // trace, roll H_prev) for `batch` solves; fix_mode: 0 never, 1 after step>1
-// if flag (FE), 2 if step (CFE with flag / SSP3 / RK4).
+// if flag (FE), 2 if step (CFE with flag / SSP3 / RK4).  The trace records
+// steps 0 .. trace_cap - 1, or with keep_last the last trace_cap steps (step
+// r in slot r mod trace_cap).
 edb_status launch_step_entropy(int N, int batch, double R, double2 *d_F, EfixState *d_state,
                                double eps, int fix_mode, double *d_trace_raw,
-                               double *d_trace_fixed, int trace_cap, cudaStream_t st);
+                               double *d_trace_fixed, int trace_cap, cudaStream_t st,
+                               bool keep_last = false);
 // EntropyFix primitives on one array (host API wrappers).
 edb_status launch_efix_average(int Nf, const double *d_f, EfixState *d_state, cudaStream_t st);
 edb_status launch_efix_entropy(int Nf, const double *d_f, EfixState *d_state, double eps,
@@ -273,7 +276,7 @@ edb_status launch_project_moments(int N, int S, const double *d_tab, double2 *d_
 edb_status launch_step_entropy_conserve(int N, int batch, double R, double2 *d_F,
                                         EfixState *d_state, double eps, int fix_mode,
                                         double *d_trace_raw, double *d_trace_fixed,
-                                        int trace_cap, cudaStream_t st);
+                                        int trace_cap, cudaStream_t st, bool keep_last = false);
 edb_status launch_maxwellian_fit(int N, int S, double R, double2 *d_F, double *d_theta,
                                  int *d_status, cudaStream_t st);
 edb_status launch_state_from_entropy(int S, const double *d_H, EfixState *d_state,

@@ -669,12 +669,16 @@ __device__ __forceinline__ void compute_line_pair(const C32Geom &g, const float 
 // wrap; the B-tile row pointer advances by one row pitch per l3 step.  With
 // the per-step index wrap and the row multiply gone, fewer integer
 // multiply-adds compete with the packed math for the FMA pipe.
-template <int A>
+// RC > 0: N = RC A known at compile time (the workload sizes, see
+// compute_line_al_n); the line's RC groups are then unrolled, so loads of one
+// group are scheduled under the arithmetic of the one before (4096 x N = 24:
+// 104 -> 99 ms).
+template <int A, int RC = 0>
 __device__ __forceinline__ void compute_line_al(const C32Geom &g, const float *Bt,
                                                 const float2 *fl0, const float2 *fl1,
                                                 const float2 *p0, const float2 *p1, int k3_0,
                                                 u64 (&accA)[A][SC], u64 (&accB)[A][SC]) {
-  const int N = g.N;
+  const int N = RC > 0 ? RC * A : g.N;
   const uint32_t sp0 = s_addr(p0), sp1 = s_addr(p1);
   uint32_t sf0 = s_addr(fl0), sf1 = s_addr(fl1), bB = s_addr(Bt);
   const uint32_t brow = 4u * g.BROW;
@@ -688,7 +692,8 @@ __device__ __forceinline__ void compute_line_al(const C32Geom &g, const float *B
     }
   }
   int base = k3_0;
-  for (int gg = 0; gg < g.R; ++gg) {
+#pragma unroll(RC > 0 ? RC : 1)
+  for (int gg = 0; gg < (RC > 0 ? RC : g.R); ++gg) {
     const int qq = base == 0 ? N : base;
     const uint32_t t0a = sp0 + 8u * base, t0b = sp1 + 8u * base;
     const uint32_t qa = sp0 + 8u * qq, qb = sp1 + 8u * qq;
@@ -733,11 +738,11 @@ __device__ __forceinline__ void compute_line_al(const C32Geom &g, const float *B
   }
 }
 
-template <int A>
+template <int A, int RC = 0>
 __device__ __forceinline__ void compute_line_pair_al(const C32Geom &g, const float *Bt,
                                                      const float2 *fl, const float2 *p, int k3_0,
                                                      u64 (&accA)[A][SC], u64 (&accB)[A][SC]) {
-  const int N = g.N;
+  const int N = RC > 0 ? RC * A : g.N;
   const uint32_t sp = s_addr(p);
   uint32_t sf = s_addr(fl), bB = s_addr(Bt);
   const uint32_t brow = 4u * g.BROW;
@@ -748,7 +753,8 @@ __device__ __forceinline__ void compute_line_pair_al(const C32Geom &g, const flo
     for (int a = 0; a < A; ++a) ring[a] = lds_u64x2(a0 + 16u * a);
   }
   int base = k3_0;
-  for (int gg = 0; gg < g.R; ++gg) {
+#pragma unroll(RC > 0 ? RC : 1)
+  for (int gg = 0; gg < (RC > 0 ? RC : g.R); ++gg) {
     const int qq = base == 0 ? N : base;
     const uint32_t t0 = sp + 16u * base, qa = sp + 16u * qq;
 #pragma unroll
@@ -783,6 +789,38 @@ __device__ __forceinline__ void compute_line_pair_al(const C32Geom &g, const flo
     base -= A;
     if (base < 0) base += N;
   }
+}
+
+// The aligned lines with N fixed at compile time for the workload sizes
+// N = 16, 24, 32 (the serving mix and the uniform batch), generic otherwise.
+// The branch is uniform over the CTA.
+template <int A>
+__device__ __forceinline__ void compute_line_al_n(const C32Geom &g, const float *Bt,
+                                                  const float2 *fl0, const float2 *fl1,
+                                                  const float2 *p0, const float2 *p1, int k3_0,
+                                                  u64 (&accA)[A][SC], u64 (&accB)[A][SC]) {
+  if (g.N == 24)
+    compute_line_al<A, 24 / A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
+  else if (g.N == 32)
+    compute_line_al<A, 32 / A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
+  else if (g.N == 16)
+    compute_line_al<A, 16 / A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
+  else
+    compute_line_al<A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
+}
+template <int A>
+__device__ __forceinline__ void compute_line_pair_al_n(const C32Geom &g, const float *Bt,
+                                                       const float2 *fl, const float2 *p,
+                                                       int k3_0, u64 (&accA)[A][SC],
+                                                       u64 (&accB)[A][SC]) {
+  if (g.N == 24)
+    compute_line_pair_al<A, 24 / A>(g, Bt, fl, p, k3_0, accA, accB);
+  else if (g.N == 32)
+    compute_line_pair_al<A, 32 / A>(g, Bt, fl, p, k3_0, accA, accB);
+  else if (g.N == 16)
+    compute_line_pair_al<A, 16 / A>(g, Bt, fl, p, k3_0, accA, accB);
+  else
+    compute_line_pair_al<A>(g, Bt, fl, p, k3_0, accA, accB);
 }
 
 // Solve pairs for the PAIR variants: out[P][e] = (re_2P, re_2P+1, im_2P,
@@ -878,6 +916,9 @@ __device__ __forceinline__ void calq32_cta(int N, int S, int K2T, int NST, int N
   auto line_li = [&](int j) { return plane_l1(P0 + j / N) * N + j % N; };
   const size_t plane_sz = (size_t)g.SG * g.PSTR;
   const bool ring_al = (N % A) == 0;  // compute_line*_al apply (tensor-copy path)
+  // the compile-time-N lines, except in the solve-pair variants under the
+  // 128-register cap or with the sums in shared memory (there they spill more)
+  constexpr bool FIXN = !(PAIR && (MINB == 2 || HLS));
 
   // zero the tile/line buffers once: padded rows (l3 >= N), row tails and the
   // f_l tails are never written by the copies and must read as zeros
@@ -992,7 +1033,9 @@ __device__ __forceinline__ void calq32_cta(int N, int S, int K2T, int NST, int N
     const float2 *fl0 = fls + (size_t)st * g.FSTG + (size_t)w * g.FLS;
     const float2 *p0 = plb + (size_t)pb * plane_sz + (size_t)w * g.PSTR + m2 * N * g.EL;
     if (PAIR) {
-      if (TMA && ring_al)
+      if (TMA && ring_al && FIXN)
+        compute_line_pair_al_n<A>(g, Bt, fl0, p0, k3_0, accA, accB);
+      else if (TMA && ring_al)
         compute_line_pair_al<A>(g, Bt, fl0, p0, k3_0, accA, accB);
       else if (TMA)
         compute_line_pair<true, true, A>(g, Bt, fl0, p0, k3_0, accA, accB);
@@ -1001,7 +1044,9 @@ __device__ __forceinline__ void calq32_cta(int N, int S, int K2T, int NST, int N
     } else {
       const float2 *fl1 = fl0 + (size_t)WS * g.FLS;
       const float2 *p1 = p0 + (size_t)WS * g.PSTR;
-      if (TMA && ring_al)
+      if (TMA && ring_al && FIXN)
+        compute_line_al_n<A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
+      else if (TMA && ring_al)
         compute_line_al<A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);
       else if (TMA)
         compute_line<true, true, A>(g, Bt, fl0, fl1, p0, p1, k3_0, accA, accB);

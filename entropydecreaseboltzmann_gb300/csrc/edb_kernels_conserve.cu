@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(CT)
     step_entropy_conserve_kernel(int N, double R, double vol, double R3, double2 *__restrict__ F,
                                  EfixState *__restrict__ state, double eps, int fix_mode,
                                  double *__restrict__ trace_raw, double *__restrict__ trace_fixed,
-                                 int trace_cap) {
+                                 int trace_cap, int keep_last) {
   __shared__ double red[(CW + 1) * 15];
   __shared__ double H_prev;
   __shared__ int step, rec;
@@ -387,9 +387,10 @@ __global__ void __launch_bounds__(CT)
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    if (rec < trace_cap) {
-      trace_raw[(long long)blockIdx.x * trace_cap + rec] = raw;
-      trace_fixed[(long long)blockIdx.x * trace_cap + rec] = H;
+    const int slot = keep_last ? rec % trace_cap : rec;  // as in step_entropy_kernel
+    if (slot < trace_cap) {
+      trace_raw[(long long)blockIdx.x * trace_cap + slot] = raw;
+      trace_fixed[(long long)blockIdx.x * trace_cap + slot] = H;
     }
     st->fixed = fixed;
     st->rec = rec + 1;
@@ -525,11 +526,13 @@ edb_status launch_project_moments(int N, int S, const double *d_tab, double2 *d_
 edb_status launch_step_entropy_conserve(int N, int batch, double R, double2 *d_F,
                                         EfixState *d_state, double eps, int fix_mode,
                                         double *d_trace_raw, double *d_trace_fixed,
-                                        int trace_cap, cudaStream_t st) {
+                                        int trace_cap, cudaStream_t st, bool keep_last) {
   const long long NQ = (long long)N * N * N;
   const double vol = pow(2 * R, 3.) / (double)NQ, R3 = pow(2 * R, 3);
+  if (keep_last && trace_cap < 1) return fail(EDB_EINVAL, "step entropy: empty trace");
   step_entropy_conserve_kernel<<<batch, CT, 0, st>>>(N, R, vol, R3, d_F, d_state, eps, fix_mode,
-                                                     d_trace_raw, d_trace_fixed, trace_cap);
+                                                     d_trace_raw, d_trace_fixed, trace_cap,
+                                                     keep_last ? 1 : 0);
   EDB_LAUNCHED();
   return EDB_OK;
 }

@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(RT)
     step_entropy_kernel(long long NQ, double vol, double R3, double2 *__restrict__ F,
                         EfixState *__restrict__ state, double eps, int fix_mode,
                         double *__restrict__ trace_raw, double *__restrict__ trace_fixed,
-                        int trace_cap) {
+                        int trace_cap, int keep_last) {
   __shared__ double red[RT];
   __shared__ AvgSnap snap;
   __shared__ double H_prev;
@@ -182,9 +182,11 @@ __global__ void __launch_bounds__(RT)
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    if (rec < trace_cap) {
-      trace_raw[(long long)blockIdx.x * trace_cap + rec] = raw;
-      trace_fixed[(long long)blockIdx.x * trace_cap + rec] = H;
+    // keep_last: the trace keeps the last trace_cap steps (slot rec mod cap)
+    const int slot = keep_last ? rec % trace_cap : rec;
+    if (slot < trace_cap) {
+      trace_raw[(long long)blockIdx.x * trace_cap + slot] = raw;
+      trace_fixed[(long long)blockIdx.x * trace_cap + slot] = H;
     }
     st->avg = snap.avg;
     st->avg_flag = snap.flag;
@@ -196,12 +198,15 @@ __global__ void __launch_bounds__(RT)
 
 edb_status launch_step_entropy(int N, int batch, double R, double2 *d_F, EfixState *d_state,
                                double eps, int fix_mode, double *d_trace_raw,
-                               double *d_trace_fixed, int trace_cap, cudaStream_t st) {
+                               double *d_trace_fixed, int trace_cap, cudaStream_t st,
+                               bool keep_last) {
   long long NQ = (long long)N * N * N;
   double vol = pow(2 * R, 3.) / (double)NQ;
   double R3 = pow(2 * R, 3);
+  if (keep_last && trace_cap < 1) return fail(EDB_EINVAL, "step entropy: empty trace");
   step_entropy_kernel<<<batch, RT, 0, st>>>(NQ, vol, R3, d_F, d_state, eps, fix_mode,
-                                            d_trace_raw, d_trace_fixed, trace_cap);
+                                            d_trace_raw, d_trace_fixed, trace_cap,
+                                            keep_last ? 1 : 0);
   EDB_LAUNCHED();
   return EDB_OK;
 }

@@ -512,13 +512,20 @@ edb_status complete(edb_server *s, Group &g) {
   for (size_t c0 = 0; c0 < fin.size(); c0 += XFER) {
     const int k = (int)std::min(fin.size() - c0, (size_t)XFER);
     bool want_hat = false;
+    // the result is the last step's real-space output: with the fix rule on,
+    // the step computed it (after the fix, which leaves F-hat alone, as the
+    // reference's BKW3D does); otherwise it is the transform of F-hat
+    const bool have_F = s->d.fix_entropy != 0;
     for (int j = 0; j < k; ++j) {
       const int slot = fin[c0 + (size_t)j];
       EDB_CUDA(cudaMemcpyAsync(g.xo + (size_t)j * NQ, g.Fhat + (size_t)slot * NQ,
                                sizeof(double2) * NQ, cudaMemcpyDeviceToDevice, st));
+      if (have_F)
+        EDB_CUDA(cudaMemcpyAsync(g.xF + (size_t)j * NQ, g.F + (size_t)slot * NQ,
+                                 sizeof(double2) * NQ, cudaMemcpyDeviceToDevice, st));
       want_hat |= s->reqs[(size_t)g.slot_req[(size_t)slot]].r.want_result != 0;
     }
-    EDB_TRY(launch_dft3d(g.N, k, g.xo, g.xF, nullptr, 1, 0, st));
+    if (!have_F) EDB_TRY(launch_dft3d(g.N, k, g.xo, g.xF, nullptr, 1, 0, st));
     EDB_CUDA(cudaMemcpyAsync(g.h_F, g.xF, sizeof(double2) * k * NQ, cudaMemcpyDeviceToHost, st));
     if (want_hat)
       EDB_CUDA(

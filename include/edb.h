@@ -374,12 +374,19 @@ edb_status edb_batch_load_device(edb_batch *b, const double *d_F0_real, void *st
 /* Advances every solve by nsteps steps (one CUDA graph launch per step). */
 edb_status edb_batch_step(edb_batch *b, int nsteps, void *stream);
 /* Real-space f (S x N^3 doubles) and Fhat (S x N^3 complex) to host memory;
- * either pointer may be NULL. */
+ * either pointer may be NULL.  With fix_entropy on, f after a step is the
+ * step's real-space output after the fix rule, as the reference's F after
+ * BKW3D's post-step rule (BKW.h:497-515): the fix rewrites F, not Fhat, so
+ * where it acted f differs from ifft(Fhat). */
 edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat);
-/* Real-space f (S x N^3 doubles) into device memory, stream-ordered (NULL:
- * the batch's own stream after the default stream's queued work,
- * synchronous). */
+/* Real-space f (S x N^3 doubles, as edb_batch_read) into device memory,
+ * stream-ordered (NULL: the batch's own stream after the default stream's
+ * queued work, synchronous). */
 edb_status edb_batch_read_device(edb_batch *b, double *d_F_real, void *stream);
+/* Entropy of each solve's last step before and after the fix rule (S doubles
+ * each, either may be NULL; NaN before the first step), calEntropy of the
+ * step's F (BKW.h:140-152) as the reference's trace prints them. */
+edb_status edb_batch_entropy(edb_batch *b, double *raw, double *fixed);
 /* Per-solve moments of the current state: S x 5 doubles (mass, momentum x3,
  * energy) on the velocity grid, and the entropy H (S doubles). */
 edb_status edb_batch_moments(edb_batch *b, double *moments, double *entropy);
