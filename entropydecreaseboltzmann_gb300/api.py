@@ -229,10 +229,14 @@ class fft3d:
                                  dptr(fre.view(np.float64))))
         return re
 
+    DOUBLE_FLOAT = 2  # EDB_DFT_DOUBLE_FLOAT
+
     @staticmethod
     def device(N, batch, d_in, d_out, inverse=False, fp32=False, stream=None):
+        """fp32: False / 0 complex128 data in FP64, True / 1 complex64 data,
+        fft3d.DOUBLE_FLOAT complex128 data with double-float passes."""
         check(lib.edb_fft3d_device(int(N), int(batch), devptr(d_in), devptr(d_out),
-                                   int(bool(inverse)), int(bool(fp32)), stream_ptr(stream)))
+                                   int(bool(inverse)), int(fp32), stream_ptr(stream)))
 
 
 class EntropyFix:

@@ -768,6 +768,7 @@ extern "C" edb_status edb_fft3d_ifft(int nx, int ny, int nz, double *re, const d
 extern "C" edb_status edb_fft3d_device(int N, int batch, const void *d_in, void *d_out,
                                        int inverse, int fp32, void *stream) {
   if (!d_in || !d_out || batch < 1) return fail(EDB_EINVAL, "bad argument");
+  if (fp32 < 0 || fp32 > EDB_DFT_DOUBLE_FLOAT) return fail(EDB_EINVAL, "unknown arithmetic mode");
   return launch_dft3d(N, batch, d_in, d_out, nullptr, inverse, fp32, (cudaStream_t)stream);
 }
 
@@ -1339,7 +1340,8 @@ extern "C" edb_status edb_batch_destroy(edb_batch *b) {
 // chunk as the chunks arrive).
 static edb_status batch_init_state(edb_batch *b, cudaStream_t st, bool transformed = false) {
   // Fhat = fft(F) in FP64, its FP32 copy, entropy bookkeeping reset
-  if (!transformed) EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->F, b->Fhat, nullptr, 0, 0, st));
+  if (!transformed)
+    EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->F, b->Fhat, nullptr, 0, EDB_DFT_DOUBLE_FLOAT, st));
   if (b->d.conserve) EDB_TRY(launch_hat_moments(b->d.N, b->d.S, b->ctab, b->Fhat, b->m0, st));
   EDB_TRY(launch_d2f(b->n, b->Fhat, b->in32, st));
   // pick the batched kernel's variant for this S on real data, before the
@@ -1387,8 +1389,8 @@ extern "C" edb_status edb_batch_load(edb_batch *b, const double *F0_real) {
     EDB_CUDA(cudaEventRecord(b->xev[i], b->cst));
     EDB_CUDA(cudaStreamWaitEvent(b->st, b->xev[i], 0));
     EDB_TRY(launch_real_to_complex((c1 - c0) * NQ, stage + c0 * NQ, b->F + c0 * NQ, b->st));
-    EDB_TRY(launch_dft3d(b->d.N, c1 - c0, b->F + c0 * NQ, b->Fhat + c0 * NQ, nullptr, 0, 0,
-                         b->st));
+    EDB_TRY(launch_dft3d(b->d.N, c1 - c0, b->F + c0 * NQ, b->Fhat + c0 * NQ, nullptr, 0,
+                         EDB_DFT_DOUBLE_FLOAT, b->st));
   }
   EDB_TRY(batch_init_state(b, b->st, true));
   b->f_cur = true;  // F holds the loaded data
@@ -1462,15 +1464,15 @@ static edb_status batch_step_record(edb_batch *b, cudaStream_t st) {
     // fixed F back into Fhat; the FP32 copy follows the final Fhat
     EDB_TRY(launch_project_moments(N, S, b->ctab, Fh, b->m0, st));
     if (b->d.fix_entropy) {
-      EDB_TRY(launch_dft3d(N, S, Fh, b->F, nullptr, 1, 0, st));
+      EDB_TRY(launch_dft3d(N, S, Fh, b->F, nullptr, 1, EDB_DFT_DOUBLE_FLOAT, st));
       EDB_TRY(launch_step_entropy_conserve(N, S, b->d.R, b->F, b->state, 1.0e-10, 2, b->tr_raw,
                                            b->tr_fixed, 1, st, true));
-      EDB_TRY(launch_dft3d(N, S, b->F, F[0], nullptr, 0, 0, st));
+      EDB_TRY(launch_dft3d(N, S, b->F, F[0], nullptr, 0, EDB_DFT_DOUBLE_FLOAT, st));
       EDB_TRY(launch_masked_copy(b->NQ, S, b->state, F[0], Fh, st));
     }
     EDB_TRY(launch_d2f(n, Fh, in, st));
   } else if (b->d.fix_entropy) {
-    EDB_TRY(launch_dft3d(N, S, Fh, b->F, nullptr, 1, 0, st));
+    EDB_TRY(launch_dft3d(N, S, Fh, b->F, nullptr, 1, EDB_DFT_DOUBLE_FLOAT, st));
     EDB_TRY(launch_step_entropy(N, S, b->d.R, b->F, b->state, 1.0e-10, 2, b->tr_raw, b->tr_fixed,
                                 1, st, true));
   }
@@ -1526,8 +1528,8 @@ extern "C" edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat)
       batch_chunk(b, i, &c0, &c1);
       if (c1 <= c0) break;
       if (!b->f_cur)
-        EDB_TRY(
-            launch_dft3d(b->d.N, c1 - c0, b->Fhat + c0 * NQ, b->F + c0 * NQ, nullptr, 1, 0, st));
+        EDB_TRY(launch_dft3d(b->d.N, c1 - c0, b->Fhat + c0 * NQ, b->F + c0 * NQ, nullptr, 1,
+                             EDB_DFT_DOUBLE_FLOAT, st));
       EDB_TRY(launch_complex_to_real((c1 - c0) * NQ, b->F + c0 * NQ, stage + c0 * NQ, st));
       EDB_CUDA(cudaEventRecord(b->xev[i], st));
       EDB_CUDA(cudaStreamWaitEvent(b->cst, b->xev[i], 0));
@@ -1545,7 +1547,8 @@ extern "C" edb_status edb_batch_read_device(edb_batch *b, double *d_F_real, void
   if (!b || !d_F_real) return fail(EDB_EINVAL, "null argument");
   if (!stream) EDB_TRY(batch_join_default(b));
   cudaStream_t st = stream ? (cudaStream_t)stream : b->st;
-  if (!b->f_cur) EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->Fhat, b->F, nullptr, 1, 0, st));
+  if (!b->f_cur)
+    EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->Fhat, b->F, nullptr, 1, EDB_DFT_DOUBLE_FLOAT, st));
   b->f_cur = true;
   EDB_TRY(launch_complex_to_real(b->n, b->F, d_F_real, st));
   if (!stream) EDB_CUDA(cudaStreamSynchronize(st));
@@ -1555,7 +1558,8 @@ extern "C" edb_status edb_batch_read_device(edb_batch *b, double *d_F_real, void
 extern "C" edb_status edb_batch_moments(edb_batch *b, double *moments, double *entropy) {
   if (!b) return fail(EDB_EINVAL, "null handle");
   cudaStream_t st = b->st;
-  if (!b->f_cur) EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->Fhat, b->F, nullptr, 1, 0, st));
+  if (!b->f_cur)
+    EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->Fhat, b->F, nullptr, 1, EDB_DFT_DOUBLE_FLOAT, st));
   b->f_cur = true;
   EDB_TRY(launch_moments(b->d.N, b->d.S, b->d.R, b->F, b->mom, st));
   EDB_TRY(launch_calentropy(b->d.N, b->d.S, b->d.R, b->F, b->H, st));

@@ -13,11 +13,38 @@
 // self-sorting form ping-pongs between two line buffers and leaves the result
 // in natural order.  The per-point cost is sum(r_i) complex operations instead
 // of N, e.g. 4 + 2 + 3 against 24 at N = 24.
+//
+// Three arithmetic types: double2 (FP64), float2 (FP32) and dfc, FP64 data
+// in memory with double-float arithmetic in the passes (each part an
+// unevaluated hi + lo float pair, edb_df.cuh): GB300 runs native FP64 at a
+// small fraction of its FP32 rate, and the FP64 passes of the batch's step
+// were bound by it (2.7 ms per pass at 4096 x N = 24).  Double-float keeps
+// about 2^-47 relative per operation.
+#include <type_traits>
+
+#include "edb_df.cuh"
 #include "edb_internal.cuh"
 
 namespace edb {
 
+// complex double-float value: re = rh + rl, im = ih + il
+struct __align__(16) dfc {
+  float rh, rl, ih, il;
+};
+
 namespace {
+using df::fast_two_sum;
+using df::sdf_add;
+using df::sdf_mul;
+using df::sdf_neg;
+
+__device__ __forceinline__ float2 dsplit(double x) {
+  const float h = (float)x;
+  return make_float2(h, (float)(x - (double)h));
+}
+__device__ __forceinline__ dfc mk_dfc(float2 re, float2 im) { return dfc{re.x, re.y, im.x, im.y}; }
+__device__ __forceinline__ float2 dre(const dfc &a) { return make_float2(a.rh, a.rl); }
+__device__ __forceinline__ float2 dim(const dfc &a) { return make_float2(a.ih, a.il); }
 constexpr int FFT_MAX_STAGES = 16;
 constexpr int FFT_THREADS = 256;
 
@@ -68,6 +95,83 @@ __device__ __forceinline__ R2 c_mul(R2 a, R2 w) {
   r.y = a.x * w.y + a.y * w.x;
   return r;
 }
+template <>
+__device__ __forceinline__ dfc c_add<dfc>(dfc a, dfc b) {
+  return mk_dfc(sdf_add(dre(a), dre(b)), sdf_add(dim(a), dim(b)));
+}
+template <>
+__device__ __forceinline__ dfc c_sub<dfc>(dfc a, dfc b) {
+  return mk_dfc(sdf_add(dre(a), sdf_neg(dre(b))), sdf_add(dim(a), sdf_neg(dim(b))));
+}
+template <>
+__device__ __forceinline__ dfc c_mul<dfc>(dfc a, dfc w) {
+  return mk_dfc(sdf_add(sdf_mul(dre(a), dre(w)), sdf_neg(sdf_mul(dim(a), dim(w)))),
+                sdf_add(sdf_mul(dre(a), dim(w)), sdf_mul(dim(a), dre(w))));
+}
+// sign i t (sign = +-1): exact
+template <typename R2>
+__device__ __forceinline__ R2 c_rot(R2 t, int sign) {
+  R2 d;
+  d.x = -sign * t.y;
+  d.y = sign * t.x;
+  return d;
+}
+template <>
+__device__ __forceinline__ dfc c_rot<dfc>(dfc t, int sign) {
+  return sign > 0 ? dfc{-t.ih, -t.il, t.rh, t.rl} : dfc{t.ih, t.il, -t.rh, -t.rl};
+}
+// radix-3 parts: t = v0 - s / 2, u = i h d (h real)
+template <typename R2>
+__device__ __forceinline__ void r3_parts(R2 v0, R2 sm, R2 df, R2 hw, R2 &t, R2 &u) {
+  const auto h = hw.y;
+  t.x = v0.x - 0.5f * sm.x;
+  t.y = v0.y - 0.5f * sm.y;
+  u.x = -h * df.y;
+  u.y = h * df.x;
+}
+template <>
+__device__ __forceinline__ void r3_parts<dfc>(dfc v0, dfc sm, dfc df, dfc hw, dfc &t, dfc &u) {
+  const float2 h = dim(hw);
+  // halving is exact in both parts
+  t = mk_dfc(sdf_add(dre(v0), make_float2(-0.5f * sm.rh, -0.5f * sm.rl)),
+             sdf_add(dim(v0), make_float2(-0.5f * sm.ih, -0.5f * sm.il)));
+  u = mk_dfc(sdf_neg(sdf_mul(h, dim(df))), sdf_mul(h, dre(df)));
+}
+// memory element <-> working value
+template <typename R2, typename G>
+__device__ __forceinline__ R2 to_work(G g) {
+  return g;
+}
+template <>
+__device__ __forceinline__ dfc to_work<dfc, double2>(double2 g) {
+  return mk_dfc(dsplit(g.x), dsplit(g.y));
+}
+// times a real scale (1 or 1/N^3), then to memory
+template <typename R2, typename R, typename G>
+__device__ __forceinline__ G from_work(R2 x, R scale) {
+  x.x *= scale;
+  x.y *= scale;
+  return x;
+}
+template <>
+__device__ __forceinline__ double2 from_work<dfc, double, double2>(dfc x, double scale) {
+  if (scale != 1.0) {
+    const float2 sc = dsplit(scale);
+    x = mk_dfc(sdf_mul(dre(x), sc), sdf_mul(dim(x), sc));
+  }
+  return make_double2((double)x.rh + (double)x.rl, (double)x.ih + (double)x.il);
+}
+template <typename R2>
+__device__ __forceinline__ R2 make_tw(double c, double s) {
+  R2 w;
+  w.x = (decltype(w.x))c;
+  w.y = (decltype(w.y))s;
+  return w;
+}
+template <>
+__device__ __forceinline__ dfc make_tw<dfc>(double c, double s) {
+  return mk_dfc(dsplit(c), dsplit(s));
+}
 
 // One Stockham stage of radix R (2, 3 or 4) on every line of the tile:
 // butterfly j of a line reads src[j + i M] (M = N / R), applies the input
@@ -94,22 +198,15 @@ __device__ __forceinline__ void fft_stage_pow2(int N, int LS, int Ns, int sign, 
       // w3 = exp(sign 2 pi i / 3) = (-1/2, h), h = tw[N / 3].y = sign sqrt(3)/2:
       // o0 = v0 + s, o1,2 = v0 - s/2 +- i h d  (s = v1 + v2, d = v1 - v2)
       const R2 sm = c_add(v[1], v[2]), df = c_sub(v[1], v[2]);
-      const auto h = tw[N / 3].y;
       R2 t, u;
-      t.x = v[0].x - 0.5f * sm.x;
-      t.y = v[0].y - 0.5f * sm.y;
-      u.x = -h * df.y;
-      u.y = h * df.x;
+      r3_parts(v[0], sm, df, tw[N / 3], t, u);
       dl[d0] = c_add(v[0], sm);
       dl[d0 + Ns] = c_add(t, u);
       dl[d0 + 2 * Ns] = c_sub(t, u);
     } else {
       // w4 = exp(sign 2 pi i / 4) = sign i; (v1 - v3) w4
       const R2 a = c_add(v[0], v[2]), b = c_sub(v[0], v[2]), c = c_add(v[1], v[3]);
-      const R2 t = c_sub(v[1], v[3]);
-      R2 d;
-      d.x = -sign * t.y;
-      d.y = sign * t.x;
+      const R2 d = c_rot(c_sub(v[1], v[3]), sign);
       dl[d0] = c_add(a, c);
       dl[d0 + Ns] = c_add(b, d);
       dl[d0 + 2 * Ns] = c_sub(a, c);
@@ -131,19 +228,29 @@ __device__ __forceinline__ void fft_stage_direct(int N, int LS, int Rd, int Ns, 
     const int k = p % Ns, rest = p / Ns;
     const int q = rest % Rd, j = (rest / Rd) * Ns + k;
     const int step = (N / (Ns * Rd)) * k + q * M;
-    R sr = 0, si = 0;
-    int m = 0;
-    for (int i = 0; i < Rd; ++i) {
-      const R2 x = sl[j + i * M];
-      const R2 w = tw[m];
-      sr += x.x * w.x - x.y * w.y;
-      si += x.x * w.y + x.y * w.x;
-      m += step;
-      if (m >= N) m %= N;
-    }
     R2 o;
-    o.x = sr;
-    o.y = si;
+    if constexpr (std::is_same<R2, dfc>::value) {
+      o = dfc{0.f, 0.f, 0.f, 0.f};
+      int m = 0;
+      for (int i = 0; i < Rd; ++i) {
+        o = c_add(o, c_mul(sl[j + i * M], tw[m]));
+        m += step;
+        if (m >= N) m %= N;
+      }
+    } else {
+      R sr = 0, si = 0;
+      int m = 0;
+      for (int i = 0; i < Rd; ++i) {
+        const R2 x = sl[j + i * M];
+        const R2 w = tw[m];
+        sr += x.x * w.x - x.y * w.y;
+        si += x.x * w.y + x.y * w.x;
+        m += step;
+        if (m >= N) m %= N;
+      }
+      o.x = sr;
+      o.y = si;
+    }
     dst[(size_t)line * LS + p] = o;
   }
 }
@@ -157,9 +264,9 @@ __device__ __forceinline__ void fft_stage_direct(int N, int LS, int Rd, int Ns, 
 // columns does not hit one bank) and the twiddle table.  in may alias out
 // (passes 2 and 3 run in place): every global read happens before the first
 // barrier and every write after the last.
-template <typename R2, typename R>
-__global__ void fft_pass_kernel(int N, int axis, int sign, R scale, FftPlan plan, const R2 *in,
-                                R2 *out) {
+template <typename R2, typename R, typename G>
+__global__ void fft_pass_kernel(int N, int axis, int sign, R scale, FftPlan plan, const G *in,
+                                G *out) {
   extern __shared__ unsigned char smem_raw[];
   const int LS = N + 1;
   R2 *buf0 = reinterpret_cast<R2 *>(smem_raw);  // [N][LS]
@@ -180,7 +287,7 @@ __global__ void fft_pass_kernel(int N, int axis, int sign, R scale, FftPlan plan
   // tile element (u, v): u = row, v = column (contiguous in memory)
   for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
     const int u = e / N, v = e - u * N;
-    const R2 x = in[base + (long long)u * row_stride + v];
+    const R2 x = to_work<R2, G>(in[base + (long long)u * row_stride + v]);
     if (axis == 2)
       buf0[(size_t)u * LS + v] = x;
     else
@@ -188,10 +295,7 @@ __global__ void fft_pass_kernel(int N, int axis, int sign, R scale, FftPlan plan
   }
   for (int r = threadIdx.x; r < N; r += blockDim.x) {
     const double ang = 8.0 * atan(1.0) * r / N;
-    R2 w;
-    w.x = (R)cos(ang);
-    w.y = (R)(sign * sin(ang));
-    tw[r] = w;
+    tw[r] = make_tw<R2>(cos(ang), sign * sin(ang));
   }
   __syncthreads();
   R2 *src = buf0, *dst = buf1;
@@ -214,32 +318,30 @@ __global__ void fft_pass_kernel(int N, int axis, int sign, R scale, FftPlan plan
   }
   for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
     const int u = e / N, v = e - u * N;
-    R2 x = (axis == 2) ? src[(size_t)u * LS + v] : src[(size_t)v * LS + u];
-    x.x *= scale;
-    x.y *= scale;
-    out[base + (long long)u * row_stride + v] = x;
+    const R2 x = (axis == 2) ? src[(size_t)u * LS + v] : src[(size_t)v * LS + u];
+    out[base + (long long)u * row_stride + v] = from_work<R2, R, G>(x, scale);
   }
 }
 
-template <typename R2, typename R>
-static edb_status dft3d_t(int N, int batch, const R2 *in, R2 *out, int inverse, cudaStream_t st) {
+template <typename R2, typename R, typename G>
+static edb_status dft3d_t(int N, int batch, const G *in, G *out, int inverse, cudaStream_t st) {
   if (N < 1 || N > 64) return fail(EDB_EINVAL, "dft3d: N out of range [1,64]");
   const int sign = inverse ? +1 : -1;
   const int threads = N * N < FFT_THREADS ? ((N * N + 31) / 32) * 32 : FFT_THREADS;
   const size_t smem = sizeof(R2) * (2 * (size_t)N * (N + 1) + N);
   // once per instantiation, thread-safe (N = 64 in FP64 needs 131 KB)
   static const cudaError_t configured = cudaFuncSetAttribute(
-      fft_pass_kernel<R2, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      fft_pass_kernel<R2, R, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   if (configured != cudaSuccess) return cuda_fail(configured, "cudaFuncSetAttribute(fft_pass)");
   const FftPlan plan = fft_plan(N);
   dim3 grid((unsigned)N, (unsigned)batch);
   const R one = (R)1;
   const R scale = inverse ? (R)(1. / ((double)N * N * N)) : one;
-  fft_pass_kernel<R2, R><<<grid, threads, smem, st>>>(N, 2, sign, one, plan, in, out);
+  fft_pass_kernel<R2, R, G><<<grid, threads, smem, st>>>(N, 2, sign, one, plan, in, out);
   EDB_LAUNCHED();
-  fft_pass_kernel<R2, R><<<grid, threads, smem, st>>>(N, 1, sign, one, plan, out, out);
+  fft_pass_kernel<R2, R, G><<<grid, threads, smem, st>>>(N, 1, sign, one, plan, out, out);
   EDB_LAUNCHED();
-  fft_pass_kernel<R2, R><<<grid, threads, smem, st>>>(N, 0, sign, scale, plan, out, out);
+  fft_pass_kernel<R2, R, G><<<grid, threads, smem, st>>>(N, 0, sign, scale, plan, out, out);
   EDB_LAUNCHED();
   return EDB_OK;
 }
@@ -247,9 +349,14 @@ static edb_status dft3d_t(int N, int batch, const R2 *in, R2 *out, int inverse, 
 edb_status launch_dft3d(int N, int batch, const void *d_in, void *d_out, void *d_tmp, int inverse,
                         int fp32, cudaStream_t st) {
   (void)d_tmp;
+  if (fp32 == EDB_DFT_DOUBLE_FLOAT)
+    return dft3d_t<dfc, double, double2>(N, batch, (const double2 *)d_in, (double2 *)d_out,
+                                         inverse, st);
   if (fp32)
-    return dft3d_t<float2, float>(N, batch, (const float2 *)d_in, (float2 *)d_out, inverse, st);
-  return dft3d_t<double2, double>(N, batch, (const double2 *)d_in, (double2 *)d_out, inverse, st);
+    return dft3d_t<float2, float, float2>(N, batch, (const float2 *)d_in, (float2 *)d_out,
+                                          inverse, st);
+  return dft3d_t<double2, double, double2>(N, batch, (const double2 *)d_in, (double2 *)d_out,
+                                           inverse, st);
 }
 
 }  // namespace edb

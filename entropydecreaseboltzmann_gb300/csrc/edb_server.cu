@@ -373,15 +373,15 @@ edb_status record_step(edb_server *s, Group &g, int S, cudaStream_t st) {
   if (s->d.conserve) {
     EDB_TRY(launch_project_moments(N, S, g.ctab, Fh, g.m0, st));
     if (s->d.fix_entropy) {
-      EDB_TRY(launch_dft3d(N, S, Fh, g.F, nullptr, 1, 0, st));
+      EDB_TRY(launch_dft3d(N, S, Fh, g.F, nullptr, 1, EDB_DFT_DOUBLE_FLOAT, st));
       EDB_TRY(launch_step_entropy_conserve(N, S, g.R, g.F, g.state, 1.0e-10, 2, g.trd, g.trd, 0,
                                            st));
-      EDB_TRY(launch_dft3d(N, S, g.F, F[0], nullptr, 0, 0, st));
+      EDB_TRY(launch_dft3d(N, S, g.F, F[0], nullptr, 0, EDB_DFT_DOUBLE_FLOAT, st));
       EDB_TRY(launch_masked_copy(g.NQ, S, g.state, F[0], Fh, st));
     }
     EDB_TRY(launch_d2f(n, Fh, in, st));
   } else if (s->d.fix_entropy) {
-    EDB_TRY(launch_dft3d(N, S, Fh, g.F, nullptr, 1, 0, st));
+    EDB_TRY(launch_dft3d(N, S, Fh, g.F, nullptr, 1, EDB_DFT_DOUBLE_FLOAT, st));
     EDB_TRY(launch_step_entropy(N, S, g.R, g.F, g.state, 1.0e-10, 2, g.trd, g.trd, 0, st));
   }
   return EDB_OK;
@@ -471,7 +471,8 @@ edb_status admit(edb_server *s, Group &g, int gi) {
     cudaStream_t st = g.st;
     EDB_CUDA(cudaMemcpyAsync(g.xin, g.h_in, sizeof(double) * k * NQ, cudaMemcpyHostToDevice, st));
     EDB_TRY(launch_real_to_complex((long long)k * g.NQ, g.xin, g.F + base, st));
-    EDB_TRY(launch_dft3d(g.N, k, g.F + base, g.Fhat + base, nullptr, 0, 0, st));
+    EDB_TRY(
+        launch_dft3d(g.N, k, g.F + base, g.Fhat + base, nullptr, 0, EDB_DFT_DOUBLE_FLOAT, st));
     if (s->d.conserve)
       EDB_TRY(launch_hat_moments(g.N, k, g.ctab, g.Fhat + base, g.m0 + (size_t)g.live * 5, st));
     EDB_TRY(launch_d2f((long long)k * g.NQ, g.Fhat + base, g.in32 + base, st));
@@ -525,7 +526,7 @@ edb_status complete(edb_server *s, Group &g) {
                                  sizeof(double2) * NQ, cudaMemcpyDeviceToDevice, st));
       want_hat |= s->reqs[(size_t)g.slot_req[(size_t)slot]].r.want_result != 0;
     }
-    if (!have_F) EDB_TRY(launch_dft3d(g.N, k, g.xo, g.xF, nullptr, 1, 0, st));
+    if (!have_F) EDB_TRY(launch_dft3d(g.N, k, g.xo, g.xF, nullptr, 1, EDB_DFT_DOUBLE_FLOAT, st));
     EDB_CUDA(cudaMemcpyAsync(g.h_F, g.xF, sizeof(double2) * k * NQ, cudaMemcpyDeviceToHost, st));
     if (want_hat)
       EDB_CUDA(

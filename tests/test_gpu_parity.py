@@ -99,6 +99,30 @@ def test_fft3d_matches_oracle(edb, oracle, N):
     assert np.max(np.abs(y - oracle.fft3d(N, Xo, inverse=True))) <= 1e-13 * np.max(np.abs(x))
 
 
+@pytest.mark.parametrize("N", [2, 3, 5, 6, 8, 12, 16, 17, 21, 24, 25, 32, 64])
+def test_fft3d_double_float_matches_oracle(edb, oracle, N):
+    """The double-float passes (FP64 data, hi + lo float arithmetic; the batch
+    and the server use them): max error <= 1e-13 of max |X|, forward and
+    inverse, over a batch of three cubes."""
+    import torch
+
+    rng = np.random.default_rng(300 + N)
+    x = rng.standard_normal((3, N ** 3)) + 1j * rng.standard_normal((3, N ** 3))
+    d = torch.from_numpy(x).cuda()
+    X = torch.empty_like(d)
+    edb.fft3d.device(N, 3, d, X, inverse=False, fp32=edb.fft3d.DOUBLE_FLOAT)
+    y = torch.empty_like(d)
+    edb.fft3d.device(N, 3, X, y, inverse=True, fp32=edb.fft3d.DOUBLE_FLOAT)
+    torch.cuda.synchronize()
+    X, y = X.cpu().numpy(), y.cpu().numpy()
+    for c in range(3):
+        Xo = oracle.fft3d(N, x[c])
+        assert np.max(np.abs(X[c] - Xo)) <= 1e-13 * np.max(np.abs(Xo))
+        yo = oracle.fft3d(N, X[c], inverse=True)
+        assert np.max(np.abs(y[c] - yo)) <= 1e-13 * np.max(np.abs(yo))
+        assert np.max(np.abs(y[c] - x[c])) <= 1e-13 * np.max(np.abs(x[c]))
+
+
 @pytest.mark.parametrize("Nt", [10, 101, 1000])
 def test_entropyfix_matches_reference(edb, golden, Nt):
     """Inputs of CalQ/testEntropyFix.cpp.  There the aim H(f2) equals H of the
