@@ -44,6 +44,10 @@ namespace {
 using namespace df;
 constexpr int RUN = 4;  // outputs per thread along j3
 constexpr int THREADS = 256;
+// two CTAs per SM: at most 128 registers a thread (no spills), 16 warps per SM
+// against 7 with 186 registers; N = 24: 0.714 -> 0.476 ms, N = 32: 2.30 ->
+// 2.03 ms.  The kernel is bound by the latency of its double-float chains.
+constexpr int MINB = 2;
 
 // tc[a][q] = T[a][(a mod 4) + 4 q] * rval, split (0 past amax).
 __global__ void tc_kernel(int amax, int rl, double rval, const double *__restrict__ T,
@@ -76,7 +80,7 @@ __global__ void bs_kernel(int N, int filter, const double *__restrict__ sigma,
 
 // FIL: the filter is on (sigma3 products enter the entry).
 template <bool FIL>
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __launch_bounds__(THREADS, MINB)
     calq64f_kernel(QParams p, int J2T, int LC, int rl, const float2 *__restrict__ tc,
                    const float4 *__restrict__ bs, const float4 *__restrict__ fdf,
                    double2 *__restrict__ partial) {
