@@ -385,15 +385,35 @@ def main():
     _ = bs.read(real=True)
     torch.cuda.synchronize()
     e2e_steps = args.steps
-    e2e_clocks = ClockSampler(local)
-    e2e_clocks.start()
+    # one batch, synchronous calls: each step's copies and transforms in series
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         bs.load(h_in.numpy())
         bs.step(1)
         bs.read(real=True, out=h_out.numpy())
+    e2e_sync_value = evals_per_step * e2e_steps / (time.perf_counter() - t0)
+    # two batches in flight through the asynchronous calls: every step still
+    # copies its inputs in and its result out, and one batch's copies overlap
+    # the other's step
+    bs2 = edb.BatchSolver(q, S, L_BOX, edb.SCHEME_RK4, DT, fix_entropy=True)
+    pair = (bs, bs2)
+    h_outs = (h_out, torch.empty_like(h_in).pin_memory())
+    bs2.load(h_in.numpy())
+    bs2.step(1)
+    bs2.read(real=True, out=h_outs[1].numpy())
+    e2e_clocks = ClockSampler(local)
+    e2e_clocks.start()
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        b = pair[i % 2]
+        b.load_async(h_in.numpy())
+        b.step_async(1)
+        b.read_async(h_outs[i % 2].numpy())
+    for b in pair:
+        b.sync()
     e2e_s = time.perf_counter() - t0
     e2e_clk = e2e_clocks.stop()
+    del bs2
     e2e_value = evals_per_step * e2e_steps / e2e_s
     h2d = S * NQ * 8
     d2h = S * NQ * 8
@@ -478,7 +498,11 @@ def main():
                        "parallelism": f"replicas x{ws}"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
-                    "path": "edb_batch_load (pinned host) + edb_batch_step + edb_batch_read",
+                    "path": "two batches in flight: edb_batch_load_async (pinned host) + "
+                            "edb_batch_step_async + edb_batch_read_async (pinned host), "
+                            "edb_batch_sync at the end",
+                    "sync_value": e2e_sync_value,
+                    "sync_path": "one batch: edb_batch_load + edb_batch_step + edb_batch_read",
                     "clocks": e2e_clk},
             "gpu_launches": int(launches),
             "clocks": clk,

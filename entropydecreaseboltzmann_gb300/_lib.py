@@ -150,6 +150,10 @@ def _load():
         "edb_batch_read": (C.c_int, [_vp, _dp, _dp]),
         "edb_batch_read_device": (C.c_int, [_vp, _vp, _vp]),
         "edb_batch_entropy": (C.c_int, [_vp, _dp, _dp]),
+        "edb_batch_load_async": (C.c_int, [_vp, _dp]),
+        "edb_batch_step_async": (C.c_int, [_vp, C.c_int]),
+        "edb_batch_read_async": (C.c_int, [_vp, _dp]),
+        "edb_batch_sync": (C.c_int, [_vp]),
         "edb_cells_transport_x_device": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double,
                                                    C.c_double, _vp, _vp, _vp]),
         "edb_batch_moments": (C.c_int, [_vp, _dp, _dp]),

@@ -454,6 +454,7 @@ class BatchSolver:
         self.S = int(S)
         self.N = qcalc.N
         self.NQ = self.N ** 3
+        self._pending = []  # host buffers of queued asynchronous copies
 
     def load(self, F0_real):
         F0 = np.ascontiguousarray(F0_real, dtype=np.float64).reshape(-1)
@@ -488,6 +489,31 @@ class BatchSolver:
         if fhat:
             out.append(Fh.reshape(self.S, self.NQ))
         return out[0] if len(out) == 1 else tuple(out)
+
+    def load_async(self, F0_real):
+        """Queued load from a C-contiguous float64 host array (pinned for the
+        copies to overlap); keep it alive and unchanged until sync()."""
+        if F0_real.dtype != np.float64 or not F0_real.flags["C_CONTIGUOUS"] \
+                or F0_real.size != self.S * self.NQ:
+            raise ValueError("expected a contiguous float64 array of S x N^3")
+        self._pending.append(F0_real)
+        check(lib.edb_batch_load_async(self._h, dptr(F0_real.reshape(-1))))
+
+    def step_async(self, nsteps=1):
+        check(lib.edb_batch_step_async(self._h, int(nsteps)))
+
+    def read_async(self, out):
+        """Queued read of real-space f into a C-contiguous float64 host array
+        of S x N^3 (pinned for the copies to overlap); valid after sync()."""
+        if out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"] \
+                or out.size != self.S * self.NQ:
+            raise ValueError("out must be a contiguous float64 array of S x N^3")
+        self._pending.append(out)
+        check(lib.edb_batch_read_async(self._h, dptr(out.reshape(-1))))
+
+    def sync(self):
+        check(lib.edb_batch_sync(self._h))
+        self._pending.clear()
 
     def read_device(self, d_F_real, stream=None):
         """Real-space f (S x N^3 float64) into a device buffer (torch tensor or address)."""

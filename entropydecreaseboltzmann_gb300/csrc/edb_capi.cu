@@ -1235,6 +1235,7 @@ struct edb_batch {
   float2 *in32 = nullptr;
   float4 *pairs = nullptr;  // solve-pair copy of in32 for the pair variants
   EfixState *state = nullptr;
+  EfixState *state_init = nullptr;  // the entropy bookkeeping's initial values, S copies
   double *tr_raw = nullptr, *tr_fixed = nullptr;
   double *mom = nullptr, *H = nullptr;
   double *ctab = nullptr, *m0 = nullptr;  // conservative mode
@@ -1250,6 +1251,7 @@ struct edb_batch {
   // copy of one chunk overlaps the transforms of the next
   cudaStream_t cst = nullptr;
   cudaEvent_t xev[8] = {};
+  cudaEvent_t xdone = nullptr;  // the last D2H of a read (the staging buffer is free)
   // NULL-stream device calls: the batch's own (non-blocking) stream first
   // waits for the work the caller queued on the default stream
   cudaEvent_t join_ev = nullptr;
@@ -1283,6 +1285,9 @@ extern "C" edb_status edb_batch_create(edb_qcalc *q, const edb_batch_desc *d, ed
   if (rc == EDB_OK &&
       (e = cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming)) != cudaSuccess)
     rc = cuda_fail(e, "cudaEventCreate");
+  if (rc == EDB_OK &&
+      (e = cudaEventCreateWithFlags(&b->xdone, cudaEventDisableTiming)) != cudaSuccess)
+    rc = cuda_fail(e, "cudaEventCreate");
   if (rc == EDB_OK) rc = dalloc(&b->Fhat, n);
   if (rc == EDB_OK) rc = dalloc(&b->F, n);
   const int nstage = d->scheme == EDB_SCHEME_RK4 ? 3 : (d->scheme == EDB_SCHEME_SSP3 ? 2 : 0);
@@ -1292,6 +1297,12 @@ extern "C" edb_status edb_batch_create(edb_qcalc *q, const edb_batch_desc *d, ed
   if (rc == EDB_OK) rc = dalloc(&b->in32, n);
   if (rc == EDB_OK) rc = dalloc(&b->pairs, calq32_pair_bytes(d->N, d->S) / sizeof(float4));
   if (rc == EDB_OK) rc = dalloc(&b->state, (size_t)d->S);
+  if (rc == EDB_OK) rc = dalloc(&b->state_init, (size_t)d->S);
+  if (rc == EDB_OK) {
+    std::vector<EfixState> init((size_t)d->S, EfixState{1.0, 0, 0, 1.0, 0, 0});
+    e = cudaMemcpy(b->state_init, init.data(), sizeof(EfixState) * d->S, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpy(batch state)");
+  }
   if (rc == EDB_OK) rc = dalloc(&b->mom, (size_t)d->S * 5);
   if (rc == EDB_OK) rc = dalloc(&b->H, (size_t)d->S);
   if (rc == EDB_OK) rc = dalloc(&b->tr_raw, (size_t)d->S);
@@ -1312,6 +1323,7 @@ extern "C" edb_status edb_batch_create(edb_qcalc *q, const edb_batch_desc *d, ed
 
 extern "C" edb_status edb_batch_destroy(edb_batch *b) {
   if (!b) return EDB_OK;
+  if (b->cst) cudaStreamSynchronize(b->cst);
   if (b->st) cudaStreamSynchronize(b->st);
   if (b->exec) cudaGraphExecDestroy(b->exec);
   dfree(b->Fhat);
@@ -1321,6 +1333,7 @@ extern "C" edb_status edb_batch_destroy(edb_batch *b) {
   dfree(b->in32);
   dfree(b->pairs);
   dfree(b->state);
+  dfree(b->state_init);
   dfree(b->mom);
   dfree(b->H);
   dfree(b->tr_raw);
@@ -1330,6 +1343,7 @@ extern "C" edb_status edb_batch_destroy(edb_batch *b) {
   for (auto &ev : b->xev)
     if (ev) cudaEventDestroy(ev);
   if (b->join_ev) cudaEventDestroy(b->join_ev);
+  if (b->xdone) cudaEventDestroy(b->xdone);
   if (b->cst) cudaStreamDestroy(b->cst);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
@@ -1338,7 +1352,10 @@ extern "C" edb_status edb_batch_destroy(edb_batch *b) {
 
 // transformed: Fhat already holds fft(F) (the chunked host load does it per
 // chunk as the chunks arrive).
-static edb_status batch_init_state(edb_batch *b, cudaStream_t st, bool transformed = false) {
+// sync = false: everything is queued on st and the call returns at once
+// (after a one-time autotune, which waits).
+static edb_status batch_init_state(edb_batch *b, cudaStream_t st, bool transformed = false,
+                                   bool sync = true) {
   // Fhat = fft(F) in FP64, its FP32 copy, entropy bookkeeping reset
   if (!transformed)
     EDB_TRY(launch_dft3d(b->d.N, b->d.S, b->F, b->Fhat, nullptr, 0, EDB_DFT_DOUBLE_FLOAT, st));
@@ -1348,9 +1365,8 @@ static edb_status batch_init_state(edb_batch *b, cudaStream_t st, bool transform
   // step graph is captured (the graph bakes the choice in)
   if (b->q->c32_variant[s_bucket(b->d.S)] < 0 && !b->exec)
     EDB_TRY(autotune_c32(b->q, b->d.S, b->in32, b->Qs[0], st, 1, nullptr, b->pairs, nullptr));
-  std::vector<EfixState> init((size_t)b->d.S, EfixState{1.0, 0, 0, 1.0, 0, 0});
-  EDB_CUDA(cudaMemcpyAsync(b->state, init.data(), sizeof(EfixState) * b->d.S,
-                           cudaMemcpyHostToDevice, st));
+  EDB_CUDA(cudaMemcpyAsync(b->state, b->state_init, sizeof(EfixState) * b->d.S,
+                           cudaMemcpyDeviceToDevice, st));
   // no step yet: the last-step entropies read as NaN (all-ones bytes)
   EDB_CUDA(cudaMemsetAsync(b->tr_raw, 0xff, sizeof(double) * b->d.S, st));
   EDB_CUDA(cudaMemsetAsync(b->tr_fixed, 0xff, sizeof(double) * b->d.S, st));
@@ -1358,7 +1374,7 @@ static edb_status batch_init_state(edb_batch *b, cudaStream_t st, bool transform
     EDB_TRY(launch_calentropy(b->d.N, b->d.S, b->d.R, b->F, b->H, st));
     EDB_TRY(launch_state_from_entropy(b->d.S, b->H, b->state, st));
   }
-  EDB_CUDA(cudaStreamSynchronize(st));
+  if (sync) EDB_CUDA(cudaStreamSynchronize(st));
   return EDB_OK;
 }
 
@@ -1373,7 +1389,9 @@ static void batch_chunk(const edb_batch *b, int i, int *c0, int *c1) {
   *c1 = std::min(b->d.S, *c0 + per);
 }
 
-extern "C" edb_status edb_batch_load(edb_batch *b, const double *F0_real) {
+// Host load: chunk copies on cst, transforms on st; sync = false returns with
+// the work queued (the caller keeps F0_real unchanged until the batch syncs).
+static edb_status batch_load_host(edb_batch *b, const double *F0_real, bool sync) {
   if (!b || !F0_real) return fail(EDB_EINVAL, "null argument");
   double *stage = batch_staging(b);
   const long long NQ = b->NQ;
@@ -1392,9 +1410,17 @@ extern "C" edb_status edb_batch_load(edb_batch *b, const double *F0_real) {
     EDB_TRY(launch_dft3d(b->d.N, c1 - c0, b->F + c0 * NQ, b->Fhat + c0 * NQ, nullptr, 0,
                          EDB_DFT_DOUBLE_FLOAT, b->st));
   }
-  EDB_TRY(batch_init_state(b, b->st, true));
+  EDB_TRY(batch_init_state(b, b->st, true, sync));
   b->f_cur = true;  // F holds the loaded data
   return EDB_OK;
+}
+
+extern "C" edb_status edb_batch_load(edb_batch *b, const double *F0_real) {
+  return batch_load_host(b, F0_real, true);
+}
+
+extern "C" edb_status edb_batch_load_async(edb_batch *b, const double *F0_real) {
+  return batch_load_host(b, F0_real, false);
 }
 
 // With a NULL stream the device-pointer calls run on the batch's own stream,
@@ -1512,10 +1538,12 @@ extern "C" edb_status edb_batch_step(edb_batch *b, int nsteps, void *stream) {
   return EDB_OK;
 }
 
-extern "C" edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat) {
+// Host read; sync = false returns with the copies queued: work queued later
+// on st waits for them (they read the staging buffer the step writes).
+static edb_status batch_read_host(edb_batch *b, double *F_real, double *Fhat, bool sync) {
   if (!b) return fail(EDB_EINVAL, "null handle");
   cudaStream_t st = b->st;
-  EDB_CUDA(cudaStreamSynchronize(st));
+  if (sync) EDB_CUDA(cudaStreamSynchronize(st));
   if (Fhat)
     EDB_CUDA(cudaMemcpyAsync(Fhat, b->Fhat, sizeof(double2) * b->n, cudaMemcpyDeviceToHost, st));
   if (F_real) {  // inverse transform (unless F is current), real parts packed
@@ -1536,11 +1564,34 @@ extern "C" edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat)
       EDB_CUDA(cudaMemcpyAsync(F_real + c0 * NQ, stage + c0 * NQ, sizeof(double) * (c1 - c0) * NQ,
                                cudaMemcpyDeviceToHost, b->cst));
     }
-    EDB_CUDA(cudaStreamSynchronize(b->cst));
+    EDB_CUDA(cudaEventRecord(b->xdone, b->cst));
+    EDB_CUDA(cudaStreamWaitEvent(st, b->xdone, 0));
+    if (sync) EDB_CUDA(cudaStreamSynchronize(b->cst));
     b->f_cur = true;
   }
-  EDB_CUDA(cudaStreamSynchronize(st));
+  if (sync) EDB_CUDA(cudaStreamSynchronize(st));
   return EDB_OK;
+}
+
+extern "C" edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat) {
+  return batch_read_host(b, F_real, Fhat, true);
+}
+
+extern "C" edb_status edb_batch_read_async(edb_batch *b, double *F_real) {
+  if (!F_real) return fail(EDB_EINVAL, "null argument");
+  return batch_read_host(b, F_real, nullptr, false);
+}
+
+extern "C" edb_status edb_batch_step_async(edb_batch *b, int nsteps) {
+  if (!b) return fail(EDB_EINVAL, "null handle");
+  return edb_batch_step(b, nsteps, (void *)b->st);
+}
+
+extern "C" edb_status edb_batch_sync(edb_batch *b) {
+  if (!b) return fail(EDB_EINVAL, "null handle");
+  EDB_CUDA(cudaStreamSynchronize(b->cst));
+  EDB_CUDA(cudaStreamSynchronize(b->st));
+  return check_device_waits("batch");
 }
 
 extern "C" edb_status edb_batch_read_device(edb_batch *b, double *d_F_real, void *stream) {

@@ -383,6 +383,17 @@ edb_status edb_batch_step(edb_batch *b, int nsteps, void *stream);
  * BKW3D's post-step rule (BKW.h:497-515): the fix rewrites F, not Fhat, so
  * where it acted f differs from ifft(Fhat). */
 edb_status edb_batch_read(edb_batch *b, double *F_real, double *Fhat);
+/* Asynchronous forms (no reference counterpart): each queues its work on the
+ * batch's own streams and returns; edb_batch_sync waits for all of it.  Host
+ * buffers must stay valid and unchanged until then, and should be pinned
+ * (page-locked) for the copies to overlap other work.  Two batches driven
+ * this way overlap one's host copies with the other's steps.  The first
+ * load of a batch whose S class is untuned still waits for the autotuner.
+ * read_async: real-space f only (as edb_batch_read). */
+edb_status edb_batch_load_async(edb_batch *b, const double *F0_real);
+edb_status edb_batch_step_async(edb_batch *b, int nsteps);
+edb_status edb_batch_read_async(edb_batch *b, double *F_real);
+edb_status edb_batch_sync(edb_batch *b);
 /* Real-space f (S x N^3 doubles, as edb_batch_read) into device memory,
  * stream-ordered (NULL: the batch's own stream after the default stream's
  * queued work, synchronous). */
