@@ -971,11 +971,15 @@ __device__ __forceinline__ void calq32_cta(int N, int S, int K2T, int NST, int N
   }
   bool to = false;
   bool aborted = false;
+  // Line j = pr N + l2 of the chunk (plane l1 = plane_l1(P0 + pr)) in stage
+  // st = j mod NST, fill parity fpar = (j / NST) & 1, and m2 = (k2c - l2) mod N
+  // are advanced by counters at the end of each line, as is the issuing warp
+  // iw = jn mod nfull of the refill line jn = j + NST - 1: no integer
+  // division in the line loop.
+  int l2 = 0, pr = 0, st = 0, fpar = 0, m2 = k2c;
+  int l1 = nlines > 0 ? plane_l1(P0) : 0;
+  int iw = (NST - 1) % nfull;
   for (int j = 0; j < nlines; ++j) {
-    const int li = line_li(j);
-    const int l1 = li / N, l2 = li % N;
-    const int pr = j / N;  // plane within the chunk
-    const int st = j % NST;
     const int pb = (NPL == 2) ? (pr & 1) : 0;
     if (l2 == 0) {
       // every warp is done with the previous plane (and with its buffer)
@@ -1009,26 +1013,33 @@ __device__ __forceinline__ void calq32_cta(int N, int S, int K2T, int NST, int N
       // fall behind the rest.  Once one of its lanes has timed out the warp
       // issues nothing more: the stage's previous copy may still be landing.
       const int jn = j + NST - 1;
-      if (warp == jn % nfull && jn < nlines) {
-        const int sn = jn % NST;
-        if (j >= 1) mbar_wait(&empty[sn], (uint32_t)(((j - 1) / NST) & 1), to, wait_ns);
+      if (warp == iw && jn < nlines) {
+        // stage of line j - 1, whose fill (j - 1) / NST completes parity
+        // fpar, or fpar ^ 1 when line j starts a new round of stages
+        const int sn = st == 0 ? NST - 1 : st - 1;
+        if (j >= 1) mbar_wait(&empty[sn], (uint32_t)(st > 0 ? fpar : fpar ^ 1), to, wait_ns);
         if (!__any_sync(warp_mask(), to)) {
-          stage_line<true>(g, line_li(jn), P0 * N + jn, sn, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs,
-                           fls, full, tmap, tmB, tmF);
+          // line jn is row l2 + NST - 1 of plane pr, or of plane pr + 1 (NST <= N)
+          int l2n = l2 + NST - 1, prn = pr;
+          if (l2n >= N) {
+            l2n -= N;
+            ++prn;
+          }
+          stage_line<true>(g, plane_l1(P0 + prn) * N + l2n, P0 * N + jn, sn, k1, k2_0, k2n, u0,
+                           nval, NQ, B32, fin, Bs, fls, full, tmap, tmB, tmF);
           if (lane == 0) ++fills[sn];
         }
       }
-      mbar_wait(&full[st], (uint32_t)((j / NST) & 1), to, wait_ns);
+      mbar_wait(&full[st], (uint32_t)fpar, to, wait_ns);
     } else {
       __syncthreads();  // previous line's readers are done (single buffer)
-      stage_line<false>(g, li, P0 * N + j, st, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs, fls, full,
-                        tmap, tmB, tmF);
+      stage_line<false>(g, l1 * N + l2, P0 * N + j, st, k1, k2_0, k2n, u0, nval, NQ, B32, fin, Bs,
+                        fls, full, tmap, tmB, tmF);
       __syncthreads();
     }
 
     // ---- compute line (l1, l2)
     if (act) {
-    const int m2 = (k2c - l2 + N) % N;
     const float *Bt = Bs + (size_t)st * g.BSTG + k2l * N + k3_0;
     const float2 *fl0 = fls + (size_t)st * g.FSTG + (size_t)w * g.FLS;
     const float2 *p0 = plb + (size_t)pb * plane_sz + (size_t)w * g.PSTR + m2 * N * g.EL;
@@ -1089,6 +1100,19 @@ __device__ __forceinline__ void calq32_cta(int N, int S, int K2T, int NST, int N
         }
       }
     }
+    // advance the line counters
+    if (++st == NST) {
+      st = 0;
+      fpar ^= 1;
+    }
+    if (++l2 == N) {
+      l2 = 0;
+      m2 = k2c;
+      if (++pr < nplanes) l1 = plane_l1(P0 + pr);
+    } else {
+      m2 = m2 == 0 ? N - 1 : m2 - 1;
+    }
+    if (++iw == nfull) iw = 0;
   }
   if (!aborted && __syncthreads_or(to)) aborted = true;
   if (aborted) {
