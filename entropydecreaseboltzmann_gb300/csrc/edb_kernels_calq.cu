@@ -682,29 +682,48 @@ __device__ __forceinline__ void compute_line_al(const C32Geom &g, const float *B
   const uint32_t sp0 = s_addr(p0), sp1 = s_addr(p1);
   uint32_t sf0 = s_addr(fl0), sf1 = s_addr(fl1), bB = s_addr(Bt);
   const uint32_t brow = 4u * g.BROW;
+  // f-hat values move in 16-byte pairs: every plane row, line and stage
+  // offset is an even number of complex values here (N % 4 == 0, even
+  // paddings), so pair loads are aligned.  A quarter-warp's 8 solve lanes then
+  // hit 8 distinct 16-byte bank groups (plane pitch N^2 + 2 complex = an odd
+  // number of pairs), where single-value loads of two windows 4 apart met
+  // pairwise in the same banks.
   u64 ring[A][SC];
   {
     const uint32_t a0 = sp0 + 8u * k3_0, a1 = sp1 + 8u * k3_0;
 #pragma unroll
-    for (int a = 0; a < A; ++a) {
-      ring[a][0] = lds_u64(a0 + 8u * a);
-      ring[a][1] = lds_u64(a1 + 8u * a);
+    for (int a = 0; a < A; a += 2) {
+      const ulonglong2 v0 = lds_u64x2(a0 + 8u * a), v1 = lds_u64x2(a1 + 8u * a);
+      ring[a][0] = v0.x;
+      ring[a + 1][0] = v0.y;
+      ring[a][1] = v1.x;
+      ring[a + 1][1] = v1.y;
     }
   }
+  u64 held[SC] = {0ull, 0ull};  // f_m at qq - t for the next even step (or next group's t = 0)
   int base = k3_0;
 #pragma unroll(RC > 0 ? RC : 1)
   for (int gg = 0; gg < (RC > 0 ? RC : g.R); ++gg) {
     const int qq = base == 0 ? N : base;
-    const uint32_t t0a = sp0 + 8u * base, t0b = sp1 + 8u * base;
     const uint32_t qa = sp0 + 8u * qq, qb = sp1 + 8u * qq;
+    ulonglong2 fp0 = make_ulonglong2(0ull, 0ull), fp1 = fp0;  // f_l of steps (t, t + 1)
 #pragma unroll
     for (int t = 0; t < A; ++t) {
-      if (t > 0) {
-        ring[(A - t) % A][0] = lds_u64(qa - 8u * t);
-        ring[(A - t) % A][1] = lds_u64(qb - 8u * t);
-      } else if (gg > 0) {
-        ring[0][0] = lds_u64(t0a);
-        ring[0][1] = lds_u64(t0b);
+      // the ring entry of step t: f_m at qq - t (t = 0: base, held over)
+      if (t == 0) {
+        if (gg > 0) {
+          ring[0][0] = held[0];
+          ring[0][1] = held[1];
+        }
+      } else if (t & 1) {  // pair (qq - t - 1, qq - t)
+        const ulonglong2 v0 = lds_u64x2(qa - 8u * (t + 1)), v1 = lds_u64x2(qb - 8u * (t + 1));
+        ring[(A - t) % A][0] = v0.y;
+        ring[(A - t) % A][1] = v1.y;
+        held[0] = v0.x;
+        held[1] = v1.x;
+      } else {
+        ring[(A - t) % A][0] = held[0];
+        ring[(A - t) % A][1] = held[1];
       }
       float bv[A];
 #pragma unroll
@@ -716,7 +735,11 @@ __device__ __forceinline__ void compute_line_al(const C32Geom &g, const float *B
         bv[4 * q4 + 3] = b.w;
       }
       bB += brow;
-      const float2 f0 = lds_f2(sf0 + 8u * t), f1 = lds_f2(sf1 + 8u * t);
+      if ((t & 1) == 0) {
+        fp0 = lds_u64x2(sf0 + 8u * t);
+        fp1 = lds_u64x2(sf1 + 8u * t);
+      }
+      const float2 f0 = upk((t & 1) ? fp0.y : fp0.x), f1 = upk((t & 1) ? fp1.y : fp1.x);
       const u64 flx[SC] = {pk(f0.x, f0.x), pk(f1.x, f1.x)};
       const u64 fly[SC] = {pk(f0.y, f0.y), pk(f1.y, f1.y)};
 #pragma unroll
