@@ -228,12 +228,14 @@ __global__ void __launch_bounds__(MAXT, MINB)
   // advanced by one row per refill so the per-row path has no division
   int rf_pi = 0, rf_i2 = 0, rf_i3 = 0;
   long long rf_base = 0;
+  const float2 *rf_src = nullptr;  // source of row q + DEPTH: B2 + (rf_base + rf_i3) KC + wcol
   if (TMA && lane == 0 && DEPTH < nrows) {
     const int t = c0 + DEPTH / N;
     rf_pi = t / N;
     rf_i2 = t % N;
     rf_i3 = DEPTH % N;
     rf_base = ((long long)plane_i1(rf_pi) * N + rf_i2) * N;
+    rf_src = B2 + (rf_base + rf_i3) * p.KC + wcol;
   }
 
   if (TMA) {
@@ -319,7 +321,11 @@ __global__ void __launch_bounds__(MAXT, MINB)
           // issues nothing more, so at most one copy per slot is in flight)
           const bool bad = __any_sync(wmask, to);
           if (lane == 0 && !bad && q + DEPTH < nrows) {
-            const long long lflat = rf_base + rf_i3;
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(&mybar[slot], seg_bytes);
+            bulk_g2s(myring + (size_t)slot * 32 * RUN, rf_src, seg_bytes, &mybar[slot]);
+            // the next row is one row of the table further (KC entries) within
+            // a line; a new line restarts from its own row block
             if (++rf_i3 == N) {
               rf_i3 = 0;
               if (++rf_i2 == N) {
@@ -327,11 +333,10 @@ __global__ void __launch_bounds__(MAXT, MINB)
                 ++rf_pi;
               }
               rf_base = ((long long)plane_i1(rf_pi) * N + rf_i2) * N;
+              rf_src = B2 + rf_base * p.KC + wcol;
+            } else {
+              rf_src += p.KC;
             }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_expect_tx(&mybar[slot], seg_bytes);
-            bulk_g2s(myring + (size_t)slot * 32 * RUN, B2 + lflat * p.KC + wcol, seg_bytes,
-                     &mybar[slot]);
             ++issued;
           }
         } else if (i3 + 1 < N) {
