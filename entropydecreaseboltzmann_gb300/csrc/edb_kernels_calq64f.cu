@@ -124,11 +124,22 @@ __global__ void __launch_bounds__(THREADS, MINB)
   int cur_i1 = -1;
   bool pair = true;
   int x1 = 0, e1 = 0;
+  // line indices advanced by counters (no division per line): list plane pi
+  // with i1 = plane_i1(pi), row i2; a1, a2 = (i + sL) mod N; the FFTW index
+  // m2f = (j2 - i2) mod N of m2
+  int pi = c0 / N, i2 = c0 % N;
+  int i1 = plane_i1(pi), a1 = (i1 + p.sL) % N, a2 = (i2 + p.sL) % N;
+  int m2f = ((j2c - i2) % N + N) % N;
   for (int line = c0; line < c1; ++line) {
-    const int i1 = plane_i1(line / N), i2 = line % N;
-    const int a1 = (i1 + p.sL) % N, a2 = (i2 + p.sL) % N;
-    // FFTW index of m2 and the centred indices of m (m = k - l)
-    const int m2f = ((j2c - i2) % N + N) % N;
+    if (line > c0) {
+      if (++i2 == N) {
+        i2 = 0;
+        i1 = plane_i1(++pi);
+        a1 = (i1 + p.sL) % N;
+      }
+      a2 = (a2 + 1 == N) ? 0 : a2 + 1;
+      m2f = (m2f == 0) ? N - 1 : m2f - 1;
+    }
     if (i1 != cur_i1) {  // stage the m1-planes of f-hat and bs
       cur_i1 = i1;
       const int m1f = ((j1 - i1) % N + N) % N;

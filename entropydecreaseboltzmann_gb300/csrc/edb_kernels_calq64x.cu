@@ -267,7 +267,8 @@ __global__ void __launch_bounds__(MAXT, MINB)
   int q = 0;  // row counter within the chunk
   for (int line = c0; line < c1; ++line) {
     // line indices: i1, i2 (centred l); a1, a2 = (i + sL) mod N (f_l, FFTW
-    // order); m2 = (j2 - i2 + sM) mod N
+    // order); m2 = (j2 - i2 + sM) mod N.  Computed per line: counters kept
+    // across the loop cost registers and measured slower here.
     const int i1 = plane_i1(line / N), i2 = line % N;
     const int a1 = (i1 + p.sL) % N, a2 = (i2 + p.sL) % N;
     const int m2 = ((j2c - i2 + p.sM) % N + N) % N;
