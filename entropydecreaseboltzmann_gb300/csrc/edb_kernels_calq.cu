@@ -215,6 +215,9 @@ constexpr unsigned long long DRAIN_LIMIT_NS = 1000000000ull;
 __device__ int g_calq32_status;  // nonzero: a bounded wait ran out
 
 constexpr int MAX_ST = 4;                 // pipeline stages (l-lines in flight)
+// the 128-byte header: (2 MAX_ST + 2) barriers, MAX_ST fill counts, and at
+// byte 120 the grouped launch's current work item
+static_assert((2 * MAX_ST + 2) * 8 + MAX_ST * 4 <= 120, "shared-memory header");
 
 struct C32Geom {
   int N, A, R, RA, K2T, BROW, FLS, PSTR, NST, NPL, HLT, SG, EL;
@@ -871,8 +874,10 @@ __global__ void c32_pairs_kernel(int S, long long NQ, const float2 *__restrict__
 // autotuner picks the variant per (table, S).
 // The work of one CTA: CTA number lin of a grid of U x GY x GZ = (solve
 // groups x chunks, N, k2 tiles) CTAs over one table (see calq32_kernel).
+// Returns false when a bounded wait ran out (the CTA drained its copies and
+// set the status word); every thread returns at the same point.
 template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB, bool PAIR>
-__device__ __forceinline__ void calq32_cta(int N, int S, int K2T, int NST, int NPL, int C, int GB,
+__device__ __forceinline__ bool calq32_cta(int N, int S, int K2T, int NST, int NPL, int C, int GB,
                                            const float *__restrict__ B32,
                                            const float2 *__restrict__ fin,
                                            float2 *__restrict__ Q, float4 *__restrict__ partial,
@@ -1163,12 +1168,12 @@ __device__ __forceinline__ void calq32_cta(int N, int S, int K2T, int NST, int N
       }
     }
     __syncthreads();
-    return;
+    return false;
   }
-  if (!k_ok) return;
 #pragma unroll
   for (int c = 0; c < SC; ++c) {
     const int s = PAIR ? s0 + 2 * w + c : s0 + w + c * WS;
+    if (!k_ok) break;
     if (s >= S) continue;
     const long long o = (long long)k1 * N * N + (long long)k2 * N;
 #pragma unroll
@@ -1206,6 +1211,7 @@ __device__ __forceinline__ void calq32_cta(int N, int S, int K2T, int NST, int N
       }
     }
   }
+  return true;
 }
 
 // One table per launch: grid (solve groups x chunks, N, k2 tiles).
@@ -1223,11 +1229,13 @@ __global__ void __launch_bounds__(MAXT, MINB)
                                                gridDim.z, lin, (int)blockDim.x);
 }
 
-// Several tables in one launch (uneven N, each table shared by its solves):
-// a descriptor per table, indexed by CTA.  Table t owns the CTAs
-// [begin, begin + U GY GZ) of a 1-D grid and runs them as its own launch
-// would (same tile shape and CTA order, so the same bits); the block is the
-// largest of the tables' (a smaller table leaves its extra threads idle).
+// Several tables in one persistent launch (uneven N, each table shared by its
+// solves): a descriptor per table, indexed by work item.  Table t owns the
+// items [begin, begin + U GY GZ) of one queue, each the work of one CTA of
+// that table's own launch (same tile shape, same item order, so the same
+// bits).  A grid of resident CTAs pulls items from the queue in order until it
+// is empty; the block is the largest of the tables' (a smaller table leaves its
+// extra threads idle).
 struct C32Table {
   CUtensorMap tmB, tmF;  // 64-byte aligned
   const float *B32;
@@ -1240,18 +1248,39 @@ constexpr int C32_MULTI_MAX = 16;
 struct C32Multi {
   C32Table t[C32_MULTI_MAX];
   int ntab;
+  long long total;         // work items (CTAs of the tables' own launches)
+  unsigned long long *queue;  // next item, zero at launch
 };
 
 template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB, bool PAIR>
 __global__ void __launch_bounds__(MAXT, MINB)
     calq32_multi_kernel(const __grid_constant__ C32Multi mt, unsigned long long wait_ns) {
-  int t = 0;
-  while (t + 1 < mt.ntab && (long long)blockIdx.x >= mt.t[t + 1].begin) ++t;
-  const C32Table &d = mt.t[t];
-  calq32_cta<TMA, MAXT, HLS, WS, A, MINB, PAIR>(d.N, d.S, d.K2T, d.NST, d.NPL, 1, d.GB, d.B32,
-                                               d.fin, d.Q, nullptr, d.tmap, wait_ns, &d.tmB,
-                                               &d.tmF, d.U, d.GY, d.GZ,
-                                               (long long)blockIdx.x - d.begin, d.threads);
+  extern __shared__ __align__(128) unsigned char smem[];
+  // the item number lives in the unused tail of the 128-byte barrier header
+  // (barriers and fill counts take 96 bytes)
+  long long *next = reinterpret_cast<long long *>(smem + 120);
+  for (;;) {
+    if (threadIdx.x == 0) *next = (long long)atomicAdd(mt.queue, 1ull);
+    __syncthreads();
+    const long long item = *next;
+    if (item >= mt.total) break;
+    int t = 0;
+    while (t + 1 < mt.ntab && item >= mt.t[t + 1].begin) ++t;
+    const C32Table &d = mt.t[t];
+    const bool ok = calq32_cta<TMA, MAXT, HLS, WS, A, MINB, PAIR>(
+        d.N, d.S, d.K2T, d.NST, d.NPL, 1, d.GB, d.B32, d.fin, d.Q, nullptr, d.tmap, wait_ns,
+        &d.tmB, &d.tmF, d.U, d.GY, d.GZ, item - d.begin, d.threads);
+    if (!ok) break;  // uniform: the CTA drained its copies and set the status word
+    // every thread is done with the item; the barriers (at the start of shared
+    // memory) are invalidated before the next item initialises them again
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+      for (int i = 0; i < 2 * MAX_ST + 2; ++i)
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(s_addr(bars + i)) : "memory");
+    }
+    __syncthreads();
+  }
 }
 
 // Chunk reduction: Q = sum over chunks (in order) of hi + lo, in FP64.
@@ -1487,21 +1516,27 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
 }
 
 template <int V>
-static edb_status launch_c32_multi_v(const C32Multi &mt, unsigned blocks, int block, size_t smem,
+static edb_status launch_c32_multi_v(const C32Multi &mt, int block, size_t smem,
                                      cudaStream_t st) {
   constexpr C32Variant vr = kC32Variants[V];
   auto kern = calq32_multi_kernel<true, vr.maxt, vr.hls, vr.ws, vr.a, vr.minb, false>;
   static const cudaError_t configured = cudaFuncSetAttribute(
       kern, cudaFuncAttributeMaxDynamicSharedMemorySize, vr.minb == 2 ? 113 * 1024 : 227 * 1024);
   if (configured != cudaSuccess) return cuda_fail(configured, "cudaFuncSetAttribute(calq32 multi)");
-  kern<<<blocks, block, smem, st>>>(mt, wait_limit_ns());
+  // persistent grid: the CTAs that fit on the device at once, at most one per item
+  int occ = 0;
+  EDB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, smem));
+  if (occ < 1) return fail(EDB_EINVAL, "calq32 multi: the block does not fit on an SM");
+  const long long blocks = std::min<long long>(mt.total, (long long)occ * device_sm_count());
+  kern<<<(unsigned)blocks, block, smem, st>>>(mt, wait_limit_ns());
   EDB_LAUNCHED();
   return EDB_OK;
 }
 
 // Grouped launch: one plain-layout variant (0-4) for every table, tensor-copy
 // staging required; tables ordered by descending N (their CTAs are the
-// longest) in one 1-D grid, each table's CTAs in its own launch's order.
+// longest) in one work queue, each table's CTAs in its own launch's order,
+// served by a persistent grid.
 edb_status launch_calq32_multi(int ntab, const C32MultiIn *in, int variant, cudaStream_t st) {
   if (ntab < 1 || ntab > C32_MULTI_MAX)
     return fail(EDB_EINVAL, "calq32 multi: 1 to 16 tables per launch");
@@ -1554,13 +1589,22 @@ edb_status launch_calq32_multi(int ntab, const C32MultiIn *in, int variant, cuda
     begin += (long long)d.U * d.GY * d.GZ;
     smem = std::max(smem, su.bytes);
   }
+  mt.total = begin;
+  // the work queue's counter, stream-ordered: allocated, zeroed, used, freed
+  EDB_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&mt.queue), sizeof(unsigned long long), st));
+  EDB_CUDA(cudaMemsetAsync(mt.queue, 0, sizeof(unsigned long long), st));
+  edb_status rc;
   switch (variant) {
-    case 0: return launch_c32_multi_v<0>(mt, (unsigned)begin, block, smem, st);
-    case 1: return launch_c32_multi_v<1>(mt, (unsigned)begin, block, smem, st);
-    case 2: return launch_c32_multi_v<2>(mt, (unsigned)begin, block, smem, st);
-    case 3: return launch_c32_multi_v<3>(mt, (unsigned)begin, block, smem, st);
-    default: return launch_c32_multi_v<4>(mt, (unsigned)begin, block, smem, st);
+    case 0: rc = launch_c32_multi_v<0>(mt, block, smem, st); break;
+    case 1: rc = launch_c32_multi_v<1>(mt, block, smem, st); break;
+    case 2: rc = launch_c32_multi_v<2>(mt, block, smem, st); break;
+    case 3: rc = launch_c32_multi_v<3>(mt, block, smem, st); break;
+    default: rc = launch_c32_multi_v<4>(mt, block, smem, st); break;
   }
+  const cudaError_t fe = cudaFreeAsync(mt.queue, st);
+  if (rc != EDB_OK) return rc;
+  if (fe != cudaSuccess) return cuda_fail(fe, "cudaFreeAsync(calq32 multi queue)");
+  return EDB_OK;
 }
 
 edb_status read_calq32_status(int *status, bool clear) {

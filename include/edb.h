@@ -183,8 +183,9 @@ edb_status edb_calQ_fp64_noalloc(int N, int index_mode, const double *d_B, const
 /* Batched Q-hat for several tables in ONE launch (no reference counterpart):
  * table i is handle qs[i] (ALIASED mode, genB done, N % 4 == 0) with S[i]
  * solves in d_fin[i] / d_Qout[i] (device, layout as
- * edb_qcalc_calQ_batch_f32_device).  1 to 16 tables.  Each CTA reads its
- * table's descriptor (N, tile shape, tensor maps, buffers) by its index, so
+ * edb_qcalc_calQ_batch_f32_device).  1 to 16 tables.  A persistent grid
+ * pulls work items (the CTAs of each table's own launch) from one queue and
+ * reads each item's table descriptor (N, tile shape, tensor maps, buffers), so
  * one launch fills the GPU with a mix of tables that would each leave it
  * partly idle.  variant: a plain-layout variant 0-4 of
  * edb_qcalc_calQ_batch_f32_ex for every table, or -1 for the one the

@@ -62,3 +62,37 @@ def test_wait_timeout_is_drained_reported_and_recovers(edb):
     assert torch.equal(again, good)
     assert np.array_equal(q.calQ(None, fh[0]), good64)
     assert edb.device_status(clear=True) == 0
+
+
+def test_wait_timeout_in_the_persistent_grouped_launch(edb):
+    """The grouped launch's persistent CTAs stop pulling work items once a
+    wait of theirs runs out; the status word is set and the next launch gives
+    the earlier bits."""
+    import torch
+
+    qs, tabs = [], []
+    for N, S in ((16, 40), (8, 33)):
+        q = edb.QCalculator(N, 0, L=6.0, filter=False, index_mode=INDEX_ALIASED)
+        q.genB()
+        rng = np.random.default_rng(N)
+        f = rng.standard_normal((S, N ** 3)) + 1j * rng.standard_normal((S, N ** 3))
+        fin = torch.from_numpy(f.astype(np.complex64)).cuda()
+        qs.append(q)
+        tabs.append((q, S, fin, torch.empty_like(fin)))
+    edb.QCalculator.calQ_batch_multi(tabs, variant=4)
+    torch.cuda.synchronize()
+    good = [t[3].clone() for t in tabs]
+    assert edb.device_status(clear=True) == 0
+    edb.set_wait_limit_ns(0)
+    try:
+        edb.QCalculator.calQ_batch_multi(tabs, variant=4)
+        torch.cuda.synchronize()
+        st = edb.device_status(clear=True)
+        assert st & 1, st
+    finally:
+        edb.set_wait_limit_ns(-1)
+    edb.QCalculator.calQ_batch_multi(tabs, variant=4)
+    torch.cuda.synchronize()
+    for t, g in zip(tabs, good):
+        assert torch.equal(t[3], g)
+    assert edb.device_status(clear=True) == 0
