@@ -180,10 +180,12 @@ struct C32MultiIn {
   const float2 *fin;
   float2 *Q;
 };
-// Q-hat of several tables' solves in one launch (1 to 16 tables, each with
-// N % 4 == 0) with one plain-layout variant (0-4): the per-table results, bit
-// for bit.
-edb_status launch_calq32_multi(int ntab, const C32MultiIn *in, int variant, cudaStream_t st);
+// Q-hat of several tables' solves in one persistent launch (1 to 16 tables,
+// each with N % 4 == 0) with one plain-layout variant (0-4): the per-table
+// results, bit for bit.  queue: CTAs pull work items from an atomic counter
+// (stream-ordered allocation); otherwise they take them round-robin.
+edb_status launch_calq32_multi(int ntab, const C32MultiIn *in, int variant, cudaStream_t st,
+                               bool queue = true);
 // Reads (and optionally clears) the batched kernel's / the double-float FP64
 // kernel's status word: nonzero when a bounded wait inside it ran out.
 edb_status read_calq32_status(int *status, bool clear);

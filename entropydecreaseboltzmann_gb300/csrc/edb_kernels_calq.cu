@@ -12,6 +12,8 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <mutex>
+#include <map>
 #include <cstring>
 #include <vector>
 
@@ -1249,7 +1251,7 @@ struct C32Multi {
   C32Table t[C32_MULTI_MAX];
   int ntab;
   long long total;         // work items (CTAs of the tables' own launches)
-  unsigned long long *queue;  // next item, zero at launch
+  unsigned long long *queue;  // next item, zero at launch; null: item b + k gridDim.x
 };
 
 template <bool TMA, int MAXT, bool HLS, int WS, int A, int MINB, bool PAIR>
@@ -1259,8 +1261,12 @@ __global__ void __launch_bounds__(MAXT, MINB)
   // the item number lives in the unused tail of the 128-byte barrier header
   // (barriers and fill counts take 96 bytes)
   long long *next = reinterpret_cast<long long *>(smem + 120);
-  for (;;) {
-    if (threadIdx.x == 0) *next = (long long)atomicAdd(mt.queue, 1ull);
+  for (long long k = 0;; ++k) {
+    // items of equal cost (one table) go round-robin; a mix is served from the
+    // queue, so CTAs that finish short items early take the next ones
+    if (threadIdx.x == 0)
+      *next = mt.queue ? (long long)atomicAdd(mt.queue, 1ull)
+                       : (long long)blockIdx.x + k * (long long)gridDim.x;
     __syncthreads();
     const long long item = *next;
     if (item >= mt.total) break;
@@ -1494,6 +1500,13 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   const float2 *src = vr.pair ? reinterpret_cast<const float2 *>(d_pairs) : d_fin;
   C32Setup su;
   EDB_TRY(c32_setup(N, S, vr, C, d_B32, src, 0, &su));
+  if (!vr.pair && C == 1 && su.tma && su.maps.tmap) {
+    // one persistent grid of resident CTAs takes the launch's CTAs round-robin
+    // (same CTA work and order, so the same bits; 4096 x N = 24: 84.9 -> 83.1
+    // ms, 512 x N = 32: 56.6 -> 53.8 ms)
+    const C32MultiIn one{N, S, d_B32, d_fin, d_Q};
+    return launch_calq32_multi(1, &one, variant, st, false);
+  }
   dim3 grid((unsigned)(((S + SG - 1) / SG) * C), (unsigned)N, (unsigned)su.tiles);
   if (vr.pair) {
     const long long n = (long long)((S + 1) / 2) * N * N * N;
@@ -1523,9 +1536,25 @@ static edb_status launch_c32_multi_v(const C32Multi &mt, int block, size_t smem,
   static const cudaError_t configured = cudaFuncSetAttribute(
       kern, cudaFuncAttributeMaxDynamicSharedMemorySize, vr.minb == 2 ? 113 * 1024 : 227 * 1024);
   if (configured != cudaSuccess) return cuda_fail(configured, "cudaFuncSetAttribute(calq32 multi)");
-  // persistent grid: the CTAs that fit on the device at once, at most one per item
+  // persistent grid: the CTAs that fit on the device at once, at most one per
+  // item (the occupancy is cached per device and shape, so a launch recorded
+  // into a graph after a first direct launch makes no query)
+  static std::mutex mu;
+  static std::map<long long, int> occ_cache;
+  int dev = 0;
+  EDB_CUDA(cudaGetDevice(&dev));
+  const long long key = ((long long)dev << 40) | ((long long)block << 24) | (long long)smem;
   int occ = 0;
-  EDB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, smem));
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = occ_cache.find(key);
+    if (it != occ_cache.end()) {
+      occ = it->second;
+    } else {
+      EDB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, smem));
+      occ_cache[key] = occ;
+    }
+  }
   if (occ < 1) return fail(EDB_EINVAL, "calq32 multi: the block does not fit on an SM");
   const long long blocks = std::min<long long>(mt.total, (long long)occ * device_sm_count());
   kern<<<(unsigned)blocks, block, smem, st>>>(mt, wait_limit_ns());
@@ -1537,7 +1566,8 @@ static edb_status launch_c32_multi_v(const C32Multi &mt, int block, size_t smem,
 // staging required; tables ordered by descending N (their CTAs are the
 // longest) in one work queue, each table's CTAs in its own launch's order,
 // served by a persistent grid.
-edb_status launch_calq32_multi(int ntab, const C32MultiIn *in, int variant, cudaStream_t st) {
+edb_status launch_calq32_multi(int ntab, const C32MultiIn *in, int variant, cudaStream_t st,
+                               bool queue) {
   if (ntab < 1 || ntab > C32_MULTI_MAX)
     return fail(EDB_EINVAL, "calq32 multi: 1 to 16 tables per launch");
   if (variant < 0 || variant >= calq32_variants() || kC32Variants[variant].pair)
@@ -1591,8 +1621,12 @@ edb_status launch_calq32_multi(int ntab, const C32MultiIn *in, int variant, cuda
   }
   mt.total = begin;
   // the work queue's counter, stream-ordered: allocated, zeroed, used, freed
-  EDB_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&mt.queue), sizeof(unsigned long long), st));
-  EDB_CUDA(cudaMemsetAsync(mt.queue, 0, sizeof(unsigned long long), st));
+  mt.queue = nullptr;
+  if (queue) {
+    EDB_CUDA(
+        cudaMallocAsync(reinterpret_cast<void **>(&mt.queue), sizeof(unsigned long long), st));
+    EDB_CUDA(cudaMemsetAsync(mt.queue, 0, sizeof(unsigned long long), st));
+  }
   edb_status rc;
   switch (variant) {
     case 0: rc = launch_c32_multi_v<0>(mt, block, smem, st); break;
@@ -1601,7 +1635,7 @@ edb_status launch_calq32_multi(int ntab, const C32MultiIn *in, int variant, cuda
     case 3: rc = launch_c32_multi_v<3>(mt, block, smem, st); break;
     default: rc = launch_c32_multi_v<4>(mt, block, smem, st); break;
   }
-  const cudaError_t fe = cudaFreeAsync(mt.queue, st);
+  const cudaError_t fe = queue ? cudaFreeAsync(mt.queue, st) : cudaSuccess;
   if (rc != EDB_OK) return rc;
   if (fe != cudaSuccess) return cuda_fail(fe, "cudaFreeAsync(calq32 multi queue)");
   return EDB_OK;
