@@ -560,7 +560,7 @@ extern "C" edb_status edb_qcalc_calQ_batch_f32_device(edb_qcalc *q, int S, const
 // variants take part when the caller passes a pair buffer.
 static edb_status autotune_c32(edb_qcalc *q, int S, const float2 *d_fin, float2 *d_Qout,
                                cudaStream_t st, int C, float4 *d_partial, float4 *d_pairs,
-                               int *chosen) {
+                               int *chosen, int persist = -1) {
   cudaEvent_t e0, e1;
   EDB_CUDA(cudaEventCreate(&e0));
   EDB_CUDA(cudaEventCreate(&e1));
@@ -570,7 +570,8 @@ static edb_status autotune_c32(edb_qcalc *q, int S, const float2 *d_fin, float2 
   for (int v = 0; v < calq32_variants() && rc == EDB_OK; ++v) {
     if (calq32_pair(v) && !d_pairs) continue;
     if (calq32_group(v) < 16 && S > 64) continue;  // small groups are for few solves
-    rc = launch_calq32_batch(q->d.N, S, q->B32, d_fin, d_Qout, st, v, C, d_partial, d_pairs);
+    rc = launch_calq32_batch(q->d.N, S, q->B32, d_fin, d_Qout, st, v, C, d_partial, d_pairs,
+                             persist);
     if (rc == EDB_EINVAL) {  // this variant does not fit this N: skip it
       rc = EDB_OK;
       continue;
@@ -578,7 +579,8 @@ static edb_status autotune_c32(edb_qcalc *q, int S, const float2 *d_fin, float2 
     if (rc != EDB_OK) break;
     cudaEventRecord(e0, st);
     for (int r = 0; r < 2 && rc == EDB_OK; ++r)
-      rc = launch_calq32_batch(q->d.N, S, q->B32, d_fin, d_Qout, st, v, C, d_partial, d_pairs);
+      rc = launch_calq32_batch(q->d.N, S, q->B32, d_fin, d_Qout, st, v, C, d_partial, d_pairs,
+                               persist);
     cudaEventRecord(e1, st);
     cudaError_t e = cudaEventSynchronize(e1);
     if (e != cudaSuccess) {
@@ -603,7 +605,8 @@ static edb_status autotune_c32(edb_qcalc *q, int S, const float2 *d_fin, float2 
 namespace edb {
 edb_status qcalc_autotune_split(edb_qcalc *q, int S, const float2 *d_fin, float2 *d_Qout,
                                 cudaStream_t st, int C, float4 *d_partial) {
-  return autotune_c32(q, S, d_fin, d_Qout, st, C, d_partial, nullptr, nullptr);
+  // the serving engine launches persistent grids (see launch_calq32_batch)
+  return autotune_c32(q, S, d_fin, d_Qout, st, C, d_partial, nullptr, nullptr, 1);
 }
 }  // namespace edb
 

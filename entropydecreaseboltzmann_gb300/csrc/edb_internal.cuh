@@ -169,9 +169,14 @@ int calq32_variants();
 int calq32_group(int variant);  // solves per CTA group
 bool calq32_pair(int variant);
 size_t calq32_pair_bytes(int N, int S);
+// persist: run the plain-layout, tensor-copy launches as one persistent grid
+// (-1: only without chunks, where it is faster alone; 1: also chunked, which
+// is slower alone but overlaps better with other groups' launches: the
+// serving engine's mix, 32 -> 36 requests/s; 0: never).
 edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin,
                                float2 *d_Q, cudaStream_t st, int variant, int C = 1,
-                               float4 *d_partial = nullptr, float4 *d_pairs = nullptr);
+                               float4 *d_partial = nullptr, float4 *d_pairs = nullptr,
+                               int persist = -1);
 // One table of a grouped batched launch: S solves (fin / Q, S x N^3 float2)
 // on the FP32 pair table B32 of their (N, gamma, L).
 struct C32MultiIn {
@@ -179,6 +184,8 @@ struct C32MultiIn {
   const float *B32;
   const float2 *fin;
   float2 *Q;
+  int C = 1;                  // l1-plane chunks (C > 1: partial sums, reduced by the caller)
+  float4 *partial = nullptr;  // C x S x N^3 when C > 1
 };
 // Q-hat of several tables' solves in one persistent launch (1 to 16 tables,
 // each with N % 4 == 0) with one plain-layout variant (0-4): the per-table

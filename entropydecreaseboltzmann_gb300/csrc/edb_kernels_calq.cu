@@ -1244,7 +1244,8 @@ struct C32Table {
   const float2 *fin;
   float2 *Q;
   long long begin;
-  int N, S, K2T, NST, NPL, GB, U, GY, GZ, tmap, threads;
+  float4 *partial;  // C > 1: chunk partial sums
+  int N, S, K2T, NST, NPL, GB, U, GY, GZ, tmap, threads, C;
 };
 constexpr int C32_MULTI_MAX = 16;
 struct C32Multi {
@@ -1274,7 +1275,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
     while (t + 1 < mt.ntab && item >= mt.t[t + 1].begin) ++t;
     const C32Table &d = mt.t[t];
     const bool ok = calq32_cta<TMA, MAXT, HLS, WS, A, MINB, PAIR>(
-        d.N, d.S, d.K2T, d.NST, d.NPL, 1, d.GB, d.B32, d.fin, d.Q, nullptr, d.tmap, wait_ns,
+        d.N, d.S, d.K2T, d.NST, d.NPL, d.C, d.GB, d.B32, d.fin, d.Q, d.partial, d.tmap, wait_ns,
         &d.tmB, &d.tmF, d.U, d.GY, d.GZ, item - d.begin, d.threads);
     if (!ok) break;  // uniform: the CTA drained its copies and set the status word
     // every thread is done with the item; the barriers (at the start of shared
@@ -1490,7 +1491,7 @@ static edb_status c32_setup(int N, int S, const C32Variant &vr, int C, const flo
 
 edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin, float2 *d_Q,
                                cudaStream_t st, int variant, int C, float4 *d_partial,
-                               float4 *d_pairs) {
+                               float4 *d_pairs, int persist) {
   if (variant < 0 || variant >= calq32_variants()) variant = 0;
   if (C < 1 || C > N) return fail(EDB_EINVAL, "calq32: chunk count must be in [1, N]");
   if (C > 1 && !d_partial) return fail(EDB_EINVAL, "calq32: chunks need a partial-sum buffer");
@@ -1500,12 +1501,20 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   const float2 *src = vr.pair ? reinterpret_cast<const float2 *>(d_pairs) : d_fin;
   C32Setup su;
   EDB_TRY(c32_setup(N, S, vr, C, d_B32, src, 0, &su));
-  if (!vr.pair && C == 1 && su.tma && su.maps.tmap) {
+  if (!vr.pair && su.tma && su.maps.tmap && (persist > 0 || (persist < 0 && C == 1))) {
     // one persistent grid of resident CTAs takes the launch's CTAs round-robin
     // (same CTA work and order, so the same bits; 4096 x N = 24: 84.9 -> 83.1
     // ms, 512 x N = 32: 56.6 -> 53.8 ms)
-    const C32MultiIn one{N, S, d_B32, d_fin, d_Q};
-    return launch_calq32_multi(1, &one, variant, st, false);
+    C32MultiIn one{N, S, d_B32, d_fin, d_Q};
+    one.C = C;
+    one.partial = d_partial;
+    EDB_TRY(launch_calq32_multi(1, &one, variant, st, false));
+    if (C == 1) return EDB_OK;
+    const long long n = (long long)S * N * N * N;
+    const long long blocks = std::min<long long>((n + 255) / 256, 16LL * device_sm_count());
+    calq32_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(n, C, d_partial, d_Q);
+    EDB_LAUNCHED();
+    return EDB_OK;
   }
   dim3 grid((unsigned)(((S + SG - 1) / SG) * C), (unsigned)N, (unsigned)su.tiles);
   if (vr.pair) {
@@ -1584,7 +1593,9 @@ edb_status launch_calq32_multi(int ntab, const C32MultiIn *in, int variant, cuda
     if (in[i].S < 1 || !in[i].B32 || !in[i].fin || !in[i].Q)
       return fail(EDB_EINVAL, "calq32 multi: bad table entry");
     C32Setup su;
-    EDB_TRY(c32_setup(in[i].N, in[i].S, vr, 1, in[i].B32, in[i].fin, 0, &su));
+    if (in[i].C < 1 || in[i].C > in[i].N || (in[i].C > 1 && !in[i].partial))
+      return fail(EDB_EINVAL, "calq32 multi: bad chunk count");
+    EDB_TRY(c32_setup(in[i].N, in[i].S, vr, in[i].C, in[i].B32, in[i].fin, 0, &su));
     block = std::max(block, su.threads);
   }
   C32Multi mt;
@@ -1595,7 +1606,7 @@ edb_status launch_calq32_multi(int ntab, const C32MultiIn *in, int variant, cuda
   for (int j = 0; j < ntab; ++j) {
     const C32MultiIn &e = in[order[j]];
     C32Setup su;
-    EDB_TRY(c32_setup(e.N, e.S, vr, 1, e.B32, e.fin, block, &su));
+    EDB_TRY(c32_setup(e.N, e.S, vr, e.C, e.B32, e.fin, block, &su));
     if (!su.tma || !su.maps.tmap)
       return fail(EDB_EINVAL, "calq32 multi: every table needs the tensor-copy path (N % 4 == 0)");
     C32Table &d = mt.t[j];
@@ -1611,7 +1622,9 @@ edb_status launch_calq32_multi(int ntab, const C32MultiIn *in, int variant, cuda
     d.NST = su.NST;
     d.NPL = su.NPL;
     d.GB = su.GB;
-    d.U = (e.S + SG - 1) / SG;
+    d.U = (e.S + SG - 1) / SG * e.C;
+    d.C = e.C;
+    d.partial = e.partial;
     d.GY = e.N;
     d.GZ = su.tiles;
     d.tmap = 1;
