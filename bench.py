@@ -515,7 +515,8 @@ def main():
                                          f"{algo_bytes / 1e9:.2f} GB (table once + f-hat in, "
                                          "Q-hat out): the table streams once per block of "
                                          "solve groups, and the kernel is FP32-bound",
-                         "kernel": "calq32_kernel", "ms_per_launch": k_ms,
+                         "kernel": "calq32_multi_kernel (the persistent form of "
+                                   "calq32_kernel's CTA work)", "ms_per_launch": k_ms,
                          "flop_per_launch": 10.0 * terms,
                          # the kernel sums each symmetric pair of terms (l, k - l) once:
                          # the pair terms it executes, and their rate on the FP32 pipe

@@ -170,9 +170,10 @@ int calq32_group(int variant);  // solves per CTA group
 bool calq32_pair(int variant);
 size_t calq32_pair_bytes(int N, int S);
 // persist: run the plain-layout, tensor-copy launches as one persistent grid
-// (-1: only without chunks, where it is faster alone; 1: also chunked, which
-// is slower alone but overlaps better with other groups' launches: the
-// serving engine's mix, 32 -> 36 requests/s; 0: never).
+// pulling the CTA work items from a queue (-1: only without chunks, where it
+// is faster alone; 1: also chunked, which is slower alone but overlaps better
+// with other groups' launches: the serving engine's mix, 32 -> 36 requests/s;
+// 0: never).
 edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin,
                                float2 *d_Q, cudaStream_t st, int variant, int C = 1,
                                float4 *d_partial = nullptr, float4 *d_pairs = nullptr,

@@ -1263,8 +1263,10 @@ __global__ void __launch_bounds__(MAXT, MINB)
   // (barriers and fill counts take 96 bytes)
   long long *next = reinterpret_cast<long long *>(smem + 120);
   for (long long k = 0;; ++k) {
-    // items of equal cost (one table) go round-robin; a mix is served from the
-    // queue, so CTAs that finish short items early take the next ones
+    // from the queue, in order, so the items in flight stay together (their
+    // table slices and f-hat blocks are shared through L2) and CTAs that
+    // finish short items early take the next ones; without a queue,
+    // round-robin
     if (threadIdx.x == 0)
       *next = mt.queue ? (long long)atomicAdd(mt.queue, 1ull)
                        : (long long)blockIdx.x + k * (long long)gridDim.x;
@@ -1502,13 +1504,15 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
   C32Setup su;
   EDB_TRY(c32_setup(N, S, vr, C, d_B32, src, 0, &su));
   if (!vr.pair && su.tma && su.maps.tmap && (persist > 0 || (persist < 0 && C == 1))) {
-    // one persistent grid of resident CTAs takes the launch's CTAs round-robin
-    // (same CTA work and order, so the same bits; 4096 x N = 24: 84.9 -> 83.1
-    // ms, 512 x N = 32: 56.6 -> 53.8 ms)
+    // one persistent grid of resident CTAs pulls the launch's CTA work items
+    // from a queue, in the launch's order (same CTA work, so the same bits;
+    // 4096 x N = 24: 84.9 -> 83.0 ms).  Taken round-robin instead, the items
+    // in flight drift apart (their costs differ by k1) and the table is read
+    // from HBM twice as often (14.3 against 7.5 GB per launch).
     C32MultiIn one{N, S, d_B32, d_fin, d_Q};
     one.C = C;
     one.partial = d_partial;
-    EDB_TRY(launch_calq32_multi(1, &one, variant, st, false));
+    EDB_TRY(launch_calq32_multi(1, &one, variant, st, true));
     if (C == 1) return EDB_OK;
     const long long n = (long long)S * N * N * N;
     const long long blocks = std::min<long long>((n + 255) / 256, 16LL * device_sm_count());
