@@ -51,7 +51,7 @@ METRIC = "batched Q̂ evals/s vs plain FP64 on GB300 at BKW L∞≤1e-6; serve p
 UNIT = "Q̂ evals/s"
 S_BATCH, N_MODES, L_BOX, DT = 4096, 24, 7.0, 0.01
 WORKLOAD = "uniform batch: 4096 solves, N=24, L=7, Maxwell (gamma=0), RK4 dt=0.01, shared B table"
-TRAFFIC_BYTES = 7.506e9 + 0.458e9  # DRAM read + write of one batched-kernel launch (ncu)
+TRAFFIC_BYTES = 7.516e9 + 0.457e9  # DRAM read + write of one batched-kernel launch (ncu)
 
 
 def dist_env():
