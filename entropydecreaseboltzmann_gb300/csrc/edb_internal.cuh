@@ -169,11 +169,13 @@ int calq32_variants();
 int calq32_group(int variant);  // solves per CTA group
 bool calq32_pair(int variant);
 size_t calq32_pair_bytes(int N, int S);
-// persist: run the plain-layout, tensor-copy launches as one persistent grid
-// pulling the CTA work items from a queue (-1: only without chunks, where it
-// is faster alone; 1: also chunked, which is slower alone but overlaps better
-// with other groups' launches: the serving engine's mix, 32 -> 36 requests/s;
-// 0: never).
+// persist: run the plain-layout, tensor-copy launches as one persistent grid.
+// -1: only without chunks, where it is faster alone, with the CTA work items
+// pulled from a queue (a stream-ordered counter: the items in flight stay
+// together, and the table is read from HBM as often as by the plain grid);
+// 1: also chunked, items taken round-robin (no counter to allocate, zero and
+// free in every graph replay): slower alone, but the serving engine's groups
+// overlap better on their streams (32 -> 36 requests/s); 0: never.
 edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d_fin,
                                float2 *d_Q, cudaStream_t st, int variant, int C = 1,
                                float4 *d_partial = nullptr, float4 *d_pairs = nullptr,

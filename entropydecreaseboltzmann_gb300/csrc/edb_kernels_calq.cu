@@ -1512,7 +1512,7 @@ edb_status launch_calq32_batch(int N, int S, const float *d_B32, const float2 *d
     C32MultiIn one{N, S, d_B32, d_fin, d_Q};
     one.C = C;
     one.partial = d_partial;
-    EDB_TRY(launch_calq32_multi(1, &one, variant, st, true));
+    EDB_TRY(launch_calq32_multi(1, &one, variant, st, persist < 0));
     if (C == 1) return EDB_OK;
     const long long n = (long long)S * N * N * N;
     const long long blocks = std::min<long long>((n + 255) / 256, 16LL * device_sm_count());
