@@ -156,7 +156,10 @@ edb_status edb_qcalc_calQ_batch_f32_device(edb_qcalc *q, int S, const float *d_f
  * input, kept by the handle.  chunks > 1 splits the l1 planes into that many
  * chunks whose compensated sums are added in order in FP64; d_partial
  * (device) then holds chunks x S x N^3 x 16 bytes.  For a given chunk count
- * the result of each solve does not depend on S or the variant. */
+ * the result of each solve does not depend on S or the variant.  Without
+ * chunks, variants 0-4 on the tensor-copy path (N % 4 == 0) run as one
+ * persistent grid of resident CTAs pulling the work items from a queue (a
+ * stream-ordered counter, so the call may be recorded into a graph). */
 edb_status edb_qcalc_calQ_batch_f32_ex(edb_qcalc *q, int S, int variant, int chunks,
                                        void *d_partial, const float *d_fin, float *d_Qout,
                                        void *stream);
