@@ -21,7 +21,7 @@
 //                 bucket S = live rounded up to 4 (the batched kernel's
 //                 smallest solve group) advances every live solve by one
 //                 step; padding slots hold zero solves.  Q-hat runs chunked
-//                 over the l1 planes (a chunk count fixed per N), so a few
+//                 over the l1 planes (4 chunks, fixed per group), so a few
 //                 live solves still fill the GPU and a result does not depend
 //                 on the bucket it ran in.
 // Groups run concurrently on their own streams.  Each solve's arithmetic
@@ -146,7 +146,11 @@ long long settled(const edb_server *s) {
 }
 
 // Chunk count of the batched kernel for a table of N (fixed per N).
-int chunks_of(int N) { return N < 8 ? N : 8; }
+// l1-plane chunks of a group's batched launches, fixed per group so a result
+// does not depend on its bucket.  Measured on the serving mix (persistent
+// launches): 4 chunks 36.1-36.2 requests/s, p50 1.33 s, uneven batch 28.7 s;
+// 8 chunks 35.5-36.2, p50 1.41-1.46 s, 29.3-29.7 s; 16 chunks 33.1, 1.61 s, 30.8 s.
+int chunks_of(int N) { return N < 4 ? N : 4; }
 
 long long slot_bytes(const edb_server *s, int N) {
   // Fhat, F (complex FP64), stage arrays, FP32 Q-hat stages, FP32 input copy,
