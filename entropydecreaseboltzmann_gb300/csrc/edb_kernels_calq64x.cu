@@ -27,7 +27,9 @@
 // Pairs: with the aliased index shifts (ALIASED mode, or odd N) B2 is the
 // split symmetric pair table (b2_pair_split_kernel) and each output plane
 // visits only the l1 planes with l1 <= (k1 - l1) mod N, about half the B
-// stream; otherwise every l-line is visited with B split as it is.
+// stream; otherwise every l-line is visited with B split as it is.  When N is
+// a multiple of 4 the pair table is read by calq64p_kernel instead (the same
+// sum with neighbouring outputs in the packed lanes; see there).
 //
 // Tiling: CTA = (output plane j1, a tile of j2, all j3) x (a chunk of its
 // l-lines (i1, i2)).  Thread = (j2, run of 4 consecutive j3).  For each i1 the f-hat
@@ -152,7 +154,20 @@ __global__ void b2_pair_split_kernel(int N, const double *__restrict__ B, float2
   double v = B[i];
   if (m1 != l1) v += B[(((long long)m1 * N + m2) * N + m3) * NQ + k];
   const float h = (float)v;
-  B2[i] = make_float2(h, (float)(v - (double)h));
+  const float lo = (float)(v - (double)h);
+  if (N % RUN == 0) {
+    // output-pair layout (calq64p_kernel): each aligned group G of four
+    // entries as the halves {h0, h1, l0, l1}, {h2, h3, l2, l3}, in swapped
+    // order when bit 2 of G is set (the reader's 128-bit loads then spread
+    // over all bank groups)
+    float *o = reinterpret_cast<float *>(B2);
+    const long long half = ((i >> 1) & 1) ^ ((i >> 4) & 1);
+    const long long hp = 2 * (i & ~3ll) + half * 4 + (i & 1);
+    o[hp] = h;
+    o[hp + 2] = lo;
+  } else {
+    B2[i] = make_float2(h, lo);
+  }
 }
 
 // TMA: per-warp bulk-copy ring for B (requires contiguous, aligned warp
@@ -409,6 +424,276 @@ __global__ void __launch_bounds__(MAXT, MINB)
   }
 }
 
+// Output-pair form of calq64x_kernel (pair table, N % 4 == 0).  The f32x2
+// lanes carry two neighbouring outputs (j3, j3 + 1) instead of the (re, im)
+// parts of one, so the table's values enter the packed instructions as they
+// are stored: each thread's four entries of a row are laid out as
+// {h0, h1, l0, l1, h2, h3, l2, l3} (b2_pair_split_kernel), and no broadcast
+// pair of b is formed (the two 16-byte halves of a thread's entries are
+// stored swapped for every other run of four threads, and each thread loads
+// them in its own order, so eight consecutive lanes cover all bank groups).
+// Per term the arithmetic is the same double-float
+// sequence: u = b f_m for the real and imaginary parts of f_m, then
+//   R += f_l.re u.re + (-f_l.im) u.im,   I += f_l.re u.im + f_l.im u.re
+// with four df_axpy per output pair.  f_m comes from a shared-memory copy of
+// the m1-plane stored as neighbour pairs, E[x] = {re_h(x), re_h(x+1),
+// im_h(x), im_h(x+1)}, {re_l(x), re_l(x+1), im_l(x), im_l(x+1)} (x + 1 mod N):
+// at step i3 the pair (0, 1) reads E[x], the pair (2, 3) E[x + 2], x =
+// (j3_0 - i3 + sM) mod N, so one new entry per step and a ring of four.  The
+// hi and lo halves sit in two planes, each row stored transposed, E[x] at
+// (x mod 4) N/4 + x/4: the lanes of a row read x four apart, which then fall
+// in distinct 16-byte bank groups (at N = 32 every 128-bit load is
+// conflict-free; untransposed, eight lanes shared one group).
+// B stream: ROWS table rows per ring slot (one wait, one vote and one
+// expect_tx per slot), PDEPTH rows in flight per warp.
+constexpr int PDEPTH = 8;
+
+template <bool TMA, int MAXT, int MINB, int ROWS>
+__global__ void __launch_bounds__(MAXT, MINB)
+    calq64p_kernel(QParams p, int J2T, int LC, const float4 *__restrict__ B2p,
+                   const float4 *__restrict__ fdf, double2 *__restrict__ partial,
+                   unsigned long long wait_ns) {
+  constexpr int SLOTS = PDEPTH / ROWS;
+  static_assert(SLOTS * ROWS == PDEPTH && RUN % ROWS == 0, "ring shape");
+  extern __shared__ __align__(128) unsigned char smem64[];
+  const int N = p.N;  // == P
+  const int R4 = N / RUN;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
+  const int wthreads = min(32, (int)blockDim.x - warp * 32);
+  const unsigned wmask = wthreads == 32 ? 0xffffffffu : ((1u << wthreads) - 1u);
+  const long long NN = (long long)N * N;
+  const long long KC2 = p.KC / 2;  // float4 per table row
+  // shared memory: [nwarps][SLOTS] mbarriers; B rings [nwarps][PDEPTH rows][32
+  // threads][2 float4]; the neighbour-pair planes (hi, then lo) [N][N] float4
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem64);
+  float4 *rings = reinterpret_cast<float4 *>(smem64 + 16 * ((nwarps * SLOTS * 8 + 15) / 16));
+  float4 *ehi = rings + (TMA ? (size_t)nwarps * PDEPTH * 32 * 2 : 0);
+  float4 *elo = ehi + (size_t)N * N;
+  uint64_t *mybar = bars + warp * SLOTS;
+  float4 *myring = rings + (size_t)warp * PDEPTH * 32 * 2;
+
+  const int r = tid % R4;
+  const int j2l = tid / R4;
+  const int j1 = blockIdx.x;
+  const int j2 = blockIdx.y * J2T + j2l;
+  const bool ok = (j2l < J2T) && (j2 < N);
+  const int j2c = ok ? j2 : 0;
+  const int j3_0 = r * RUN;
+  const int chunk = blockIdx.z;
+  // l1 planes this output plane visits (the pair table): a1 <= (k1 - a1) mod N
+  const int k1f = (j1 - p.n + N) % N;
+  const int plo = k1f / 2;
+  const int nlist = plo + 1 + max(0, (k1f + N) / 2 - k1f);
+  auto plane_i1 = [&](int pi) {
+    const int a = pi <= plo ? pi : k1f + 1 + (pi - plo - 1);
+    return (a + p.n) % N;
+  };
+  const int NL = nlist * N;
+  const int c0 = min(NL, chunk * LC), c1 = min(NL, c0 + LC);
+  auto row_of = [&](int qq) -> long long {
+    const int t = c0 + qq / N;
+    return ((long long)plane_i1(t / N) * N + t % N) * N + qq % N;
+  };
+  // entry index of the thread's run within a row (a multiple of 4: float4 kcol / 2)
+  const long long kcol = ((long long)j1 * N + j2c) * N + j3_0;
+  const int hsw = (int)((kcol >> 4) & 1);  // halves stored swapped
+  const long long wcol = ((long long)j1 * N + (blockIdx.y * J2T + (warp * 32) / R4)) * N +
+                         ((warp * 32) % R4) * RUN;
+  const uint32_t seg_bytes = (uint32_t)(wthreads * RUN * sizeof(float2));
+  const int nrows = (c1 - c0) * N;  // even: N % 4 == 0
+  bool to = false;
+  int issued = 0;  // lane 0: slot fills its warp has issued
+  int rf_pi = 0, rf_i2 = 0, rf_i3 = 0;
+  const float4 *rf_src = nullptr;  // lane 0: source of the next row to issue
+  if (TMA && lane == 0 && PDEPTH < nrows) {
+    const int t = c0 + PDEPTH / N;
+    rf_pi = t / N;
+    rf_i2 = t % N;
+    rf_i3 = PDEPTH % N;
+    const long long base = ((long long)plane_i1(rf_pi) * N + rf_i2) * N;
+    rf_src = B2p + (base + rf_i3) * KC2 + wcol / 2;
+  }
+
+  if (TMA) {
+    if (lane == 0) {
+      for (int d = 0; d < SLOTS; ++d) mbar_init(&mybar[d], 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp(wmask);
+    if (lane == 0) {  // prologue: rows [0, PDEPTH)
+      for (int s = 0; s < SLOTS && s * ROWS < nrows; ++s) {
+        const int nr = min(ROWS, nrows - s * ROWS);
+        mbar_expect_tx(&mybar[s], seg_bytes * nr);
+        for (int rr = 0; rr < nr; ++rr) {
+          const int qq = s * ROWS + rr;
+          bulk_g2s(myring + (size_t)qq * 32 * 2, B2p + row_of(qq) * KC2 + wcol / 2, seg_bytes,
+                   &mybar[s]);
+        }
+        ++issued;
+      }
+    }
+  }
+
+  DF2 accR[2], accI[2];  // lanes (j3_0 + 2h, j3_0 + 2h + 1)
+#pragma unroll
+  for (int h = 0; h < 2; ++h) accR[h].h = accR[h].l = accI[h].h = accI[h].l = 0ull;
+  const u64 MONE = pk(-1.0f, -1.0f);
+
+  const int x0 = (j3_0 + p.sM) % N;  // E index of pair (0, 1) at i3 = 0
+  const int fi0 = p.sL % N;
+  int cur_i1 = -1;
+  int q = 0;
+  for (int line = c0; line < c1; ++line) {
+    const int i1 = plane_i1(line / N), i2 = line % N;
+    const int a1 = (i1 + p.sL) % N, a2 = (i2 + p.sL) % N;
+    const int m2 = ((j2c - i2 + p.sM) % N + N) % N;
+    if (i1 != cur_i1) {  // stage the m1-plane as neighbour pairs
+      cur_i1 = i1;
+      const int m1 = ((j1 - i1 + p.sM) % N + N) % N;
+      const float4 *src = fdf + (long long)m1 * NN;
+      __syncthreads();
+      for (long long e = tid; e < NN; e += blockDim.x) {
+        const long long row = e / N;
+        const int c = (int)(e - row * N);
+        const float4 v0 = src[e], v1 = src[row * N + (c + 1 == N ? 0 : c + 1)];
+        const long long d = row * N + (c & 3) * R4 + (c >> 2);
+        ehi[d] = make_float4(v0.x, v1.x, v0.y, v1.y);
+        elo[d] = make_float4(v0.z, v1.z, v0.w, v1.w);
+      }
+      __syncthreads();
+    }
+    const float4 *erh = ehi + (size_t)m2 * N, *erl = elo + (size_t)m2 * N;
+    const float4 *flrow = fdf + ((long long)a1 * N + a2) * N;
+    const long long lrow0 = ((long long)i1 * N + i2) * N;
+    // ring[s]: E entry of step i3 with i3 mod 4 = s; hi pairs (re, im), lo pairs
+    u64 eh[4][2], el[4][2];
+    auto load_e = [&](int x, int s) {
+      const int px = (x & 3) * R4 + (x >> 2);
+      const float4 u = erh[px], w = erl[px];
+      eh[s][0] = pk(u.x, u.y);
+      eh[s][1] = pk(u.z, u.w);
+      el[s][0] = pk(w.x, w.y);
+      el[s][1] = pk(w.z, w.w);
+    };
+    {
+      const int x1 = x0 + 1 < N ? x0 + 1 : x0 + 1 - N;
+      const int x2 = x1 + 1 < N ? x1 + 1 : x1 + 1 - N;
+      load_e(x0, 0);
+      load_e(x1, 3);  // E[x + 1] of step 0 = the entry of step -1
+      load_e(x2, 2);  // E[x + 2] of step 0 = the entry of step -2
+    }
+    const float4 *brow = B2p + lrow0 * KC2 + kcol / 2;
+    float4 bv0, bv1, bn0, bn1;
+    if (!TMA) {
+      bv0 = __ldg(brow + hsw);
+      bv1 = __ldg(brow + 1 - hsw);
+    }
+    int xn = x0;
+    int fi = fi0;
+    float4 fl_next = __ldg(flrow + fi);
+    for (int g = 0; g < N; g += RUN) {
+#pragma unroll
+      for (int t = 0; t < RUN; ++t, ++q) {
+        const int i3 = g + t;
+        if (TMA) {
+          const int slot = (q / ROWS) % SLOTS;
+          if (t % ROWS == 0) mbar_wait(&mybar[slot], (uint32_t)((q / PDEPTH) & 1), to, wait_ns);
+          const float4 *src = myring + ((size_t)(slot * ROWS + t % ROWS) * 32 + lane) * 2;
+          bv0 = src[hsw];
+          bv1 = src[1 - hsw];
+          if (t % ROWS == ROWS - 1) {
+            // every lane has read the slot's rows; refill it with the next
+            // ROWS rows unless a lane timed out
+            const bool bad = __any_sync(wmask, to);
+            const int first = q + 1 - ROWS + PDEPTH;
+            if (lane == 0 && !bad && first < nrows) {
+              const int nr = min(ROWS, nrows - first);
+              asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+              mbar_expect_tx(&mybar[slot], seg_bytes * nr);
+              for (int rr = 0; rr < nr; ++rr) {
+                bulk_g2s(myring + ((size_t)(slot * ROWS + rr) * 32) * 2, rf_src, seg_bytes,
+                         &mybar[slot]);
+                if (++rf_i3 == N) {
+                  rf_i3 = 0;
+                  if (++rf_i2 == N) {
+                    rf_i2 = 0;
+                    ++rf_pi;
+                  }
+                  rf_src = B2p + ((long long)plane_i1(rf_pi) * N + rf_i2) * N * KC2 + wcol / 2;
+                } else {
+                  rf_src += KC2;
+                }
+              }
+              ++issued;
+            }
+          }
+        } else if (i3 + 1 < N) {
+          const float4 *bn = brow + (long long)(i3 + 1) * KC2;
+          bn0 = __ldg(bn + hsw);
+          bn1 = __ldg(bn + 1 - hsw);
+        }
+        if (i3 > 0) {  // the new entry E[x], x = x0 - i3
+          xn = (xn == 0) ? N - 1 : xn - 1;
+          load_e(xn, t);
+        }
+        const float4 fl = fl_next;
+        fi = (fi + 1 == N) ? 0 : fi + 1;
+        fl_next = __ldg(flrow + fi);
+        const u64 xr = pk(fl.x, fl.x), nxr = pk(-fl.x, -fl.x), nlr = pk(-fl.z, -fl.z);
+        const u64 xi = pk(fl.y, fl.y), nxi = pk(-fl.y, -fl.y), nli = pk(-fl.w, -fl.w);
+        const u64 li = pk(fl.w, fl.w);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int s = (t + 2 * h) % RUN;
+          const float4 bv = h ? bv1 : bv0;
+          const u64 bh = pk(bv.x, bv.y), bl = pk(bv.z, bv.w);
+          const u64 nbh = mul2(bh, MONE);
+          // u = b f_m per part: -u_h rounded, and the exact error plus cross terms
+          const u64 nure = mul2(nbh, eh[s][0]);
+          const u64 ucre = fma2(bh, el[s][0], fma2(bl, eh[s][0], fma2(bh, eh[s][0], nure)));
+          const u64 nuim = mul2(nbh, eh[s][1]);
+          const u64 ucim = fma2(bh, el[s][1], fma2(bl, eh[s][1], fma2(bh, eh[s][1], nuim)));
+          df_axpy(accR[h], xr, nxr, nlr, nure, ucre);  // + f_l.re u.re
+          df_axpy(accR[h], nxi, xi, li, nuim, ucim);   // - f_l.im u.im
+          df_axpy(accI[h], xr, nxr, nlr, nuim, ucim);  // + f_l.re u.im
+          df_axpy(accI[h], xi, nxi, nli, nure, ucre);  // + f_l.im u.re
+        }
+        if (!TMA) {
+          bv0 = bn0;
+          bv1 = bn1;
+        }
+      }
+    }
+  }
+  if (TMA) {
+    if (__syncthreads_or(to)) {
+      if (lane == 0) {
+        atomicExch(&g_calq64x_status, 1);
+        // drain: fill f went into slot f % SLOTS, and a slot is refilled only
+        // after its previous fill landed, so only each slot's last fill can
+        // still be in flight
+        for (int sl = 0; sl < SLOTS && sl < issued; ++sl) {
+          const int last = sl + ((issued - 1 - sl) / SLOTS) * SLOTS;
+          bool t2 = false;
+          mbar_wait(&mybar[sl], (uint32_t)((last / SLOTS) & 1), t2, DRAIN_LIMIT_NS);
+        }
+      }
+      __syncwarp(wmask);
+      return;
+    }
+  }
+  if (!ok) return;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const float2 Rh = upk(accR[h].h), Rl = upk(accR[h].l);
+    const float2 Ih = upk(accI[h].h), Il = upk(accI[h].l);
+    double2 *o = partial + (long long)chunk * p.KC + kcol + 2 * h;
+    o[0] = make_double2((double)Rh.x + (double)Rl.x, (double)Ih.x + (double)Il.x);
+    o[1] = make_double2((double)Rh.y + (double)Rl.y, (double)Ih.y + (double)Il.y);
+  }
+}
+
 struct C64xPlan {
   int J2T, tiles, threads, LC, nch;
   bool tma;
@@ -424,24 +709,42 @@ struct C64xShape {
 };
 constexpr C64xShape kC64xShapes[] = {{256, 2}, {256, 1}, {128, 3}, {128, 4}, {192, 2}};
 constexpr int kC64xNShapes = (int)(sizeof(kC64xShapes) / sizeof(kC64xShapes[0]));
+// The output-pair kernel's shapes (same count): CTA size bound, CTAs per SM,
+// table rows per ring slot.  N = 32 (ms per launch): 1.27, 1.37, 1.62, 1.54
+// for the first four with 4, 2, 2, 2 rows; 1.45 with one row per slot.
+struct C64pShape {
+  int maxt, minb, rows;
+};
+constexpr C64pShape kC64pShapes[] = {{256, 2, 4}, {256, 2, 2}, {128, 3, 2}, {128, 4, 2}, {256, 2, 1}};
+static_assert(sizeof(kC64pShapes) / sizeof(kC64pShapes[0]) == kC64xNShapes, "shape count");
+// the output-pair kernel runs the pair table when N is a multiple of 4
+static bool c64_op(const QParams &p, bool paired) { return paired && p.N % RUN == 0; }
 
 template <bool TMA, int S>
-static const void *c64x_fn_s() {
+static const void *c64x_fn_s(bool op) {
+  if (op)
+    return (const void *)
+        calq64p_kernel<TMA, kC64pShapes[S].maxt, kC64pShapes[S].minb, kC64pShapes[S].rows>;
   return (const void *)calq64x_kernel<TMA, kC64xShapes[S].maxt, kC64xShapes[S].minb>;
 }
 template <bool TMA>
-static const void *c64x_fn(int shape) {
+static const void *c64x_fn(int shape, bool op) {
   switch (shape) {
-    case 0: return c64x_fn_s<TMA, 0>();
-    case 1: return c64x_fn_s<TMA, 1>();
-    case 2: return c64x_fn_s<TMA, 2>();
-    case 3: return c64x_fn_s<TMA, 3>();
-    default: return c64x_fn_s<TMA, 4>();
+    case 0: return c64x_fn_s<TMA, 0>(op);
+    case 1: return c64x_fn_s<TMA, 1>(op);
+    case 2: return c64x_fn_s<TMA, 2>(op);
+    case 3: return c64x_fn_s<TMA, 3>(op);
+    default: return c64x_fn_s<TMA, 4>(op);
   }
 }
 
-static size_t c64x_smem(int N, int threads, bool tma) {
+static size_t c64x_smem(int N, int threads, bool tma, bool op, int rows) {
   const int nwarps = (threads + 31) / 32;
+  if (op) {
+    size_t o = 16 * (size_t)((nwarps * (PDEPTH / rows) * 8 + 15) / 16);
+    if (tma) o += 2 * sizeof(float4) * (size_t)nwarps * PDEPTH * 32;
+    return o + 2 * sizeof(float4) * (size_t)N * N;
+  }
   size_t o = 16 * (size_t)((nwarps * DEPTH * 8 + 15) / 16);
   if (tma) o += sizeof(float2) * (size_t)nwarps * DEPTH * 32 * RUN;
   return o + sizeof(float4) * (size_t)N * N;
@@ -477,8 +780,9 @@ static C64xPlan c64x_plan(const QParams &p, bool aligned, int shape, bool paired
 
 static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int shape, bool paired) {
   C64xPlan pl;
+  const bool op = c64_op(p, paired);
   const int R4 = (p.P + RUN - 1) / RUN;
-  int J2T = std::max(1, kC64xShapes[shape].maxt / R4);
+  int J2T = std::max(1, (op ? kC64pShapes[shape].maxt : kC64xShapes[shape].maxt) / R4);
   if (J2T > p.P) J2T = p.P;
   const int tiles = (p.P + J2T - 1) / J2T;
   J2T = (p.P + tiles - 1) / tiles;
@@ -486,9 +790,9 @@ static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int shape, boo
   pl.tiles = tiles;
   pl.threads = J2T * R4;
   pl.tma = aligned && (p.P % RUN) == 0 && (p.P % J2T) == 0;
-  pl.smem = c64x_smem(p.N, pl.threads, pl.tma);
+  pl.smem = c64x_smem(p.N, pl.threads, pl.tma, op, kC64pShapes[shape].rows);
   int occ = 1;
-  const void *fn = pl.tma ? c64x_fn<true>(shape) : c64x_fn<false>(shape);
+  const void *fn = pl.tma ? c64x_fn<true>(shape, op) : c64x_fn<false>(shape, op);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, pl.threads, pl.smem);
   if (occ < 1) occ = 1;
@@ -556,9 +860,15 @@ template <bool TMA, int S>
 static void c64x_launch_s(dim3 grid, const C64xPlan &pl, const QParams &p, bool paired,
                           const float2 *d_B2, const float4 *d_fdf, double2 *d_partial,
                           cudaStream_t st) {
-  calq64x_kernel<TMA, kC64xShapes[S].maxt, kC64xShapes[S].minb>
-      <<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf, d_partial,
-                                          wait_limit_ns());
+  if (c64_op(p, paired))
+    calq64p_kernel<TMA, kC64pShapes[S].maxt, kC64pShapes[S].minb, kC64pShapes[S].rows>
+        <<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC,
+                                            reinterpret_cast<const float4 *>(d_B2), d_fdf,
+                                            d_partial, wait_limit_ns());
+  else
+    calq64x_kernel<TMA, kC64xShapes[S].maxt, kC64xShapes[S].minb>
+        <<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf, d_partial,
+                                            wait_limit_ns());
 }
 template <bool TMA>
 static void c64x_launch(int shape, dim3 grid, const C64xPlan &pl, const QParams &p, bool paired,
@@ -580,6 +890,8 @@ edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const float4 *d_
   if (paired && (p.P != p.N || (p.sM % p.N) != 0 || (p.sL % p.N) != p.N - p.n))
     return fail(EDB_EINVAL, "calq64x: pairs need the aliased index shifts");
   const bool aligned = ((uintptr_t)d_B2 % 16) == 0;
+  if (c64_op(p, paired) && !aligned)
+    return fail(EDB_EINVAL, "calq64x: the output-pair table must be 16-byte aligned");
   const C64xPlan pl = c64x_plan(p, aligned, shape, paired);
   dim3 grid((unsigned)p.P, (unsigned)pl.tiles, (unsigned)pl.nch);
   if (pl.tma)
