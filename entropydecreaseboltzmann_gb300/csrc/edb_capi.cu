@@ -251,7 +251,7 @@ static edb_status qcalc_alloc_work(edb_qcalc *q) {
     EDB_TRY(dalloc(&q->partial, (size_t)nmax * q->p.KC));
   }
 
-  if (!q->fdf) EDB_TRY(dalloc(&q->fdf, (size_t)q->p.NQ));  // split f
+  if (!q->fdf) EDB_TRY(dalloc(&q->fdf, (size_t)q->p.NQ + 1));  // split f (+ padding)
   if (!q->fin) EDB_TRY(dalloc(&q->fin, (size_t)q->p.NQ));
   if (!q->Q) EDB_TRY(dalloc(&q->Q, (size_t)q->p.NQ));
   return EDB_OK;
@@ -264,7 +264,6 @@ static edb_status qcalc_tune_fp64(edb_qcalc *q) {
   if (!q->B2) return EDB_OK;
   cudaStream_t st = q->st;
   EDB_CUDA(cudaMemsetAsync(q->fin, 0, sizeof(double2) * q->p.NQ, st));
-  EDB_TRY(launch_split_f(q->p.NQ, q->fin, q->fdf, st));
   cudaEvent_t e0, e1;
   EDB_CUDA(cudaEventCreate(&e0));
   EDB_CUDA(cudaEventCreate(&e1));
@@ -272,10 +271,12 @@ static edb_status qcalc_tune_fp64(edb_qcalc *q) {
   int best_shape = 0;
   edb_status rc = EDB_OK;
   for (int shape = 0; shape < calq64x_shapes() && rc == EDB_OK; ++shape) {
-    rc = launch_calq64x(q->p, q->B2, q->fdf, q->partial, q->Q, st, shape, qcalc_b2_paired(q));
+    rc = launch_calq64x(q->p, q->B2, q->fin, q->fdf, q->partial, q->Q, st, shape,
+                        qcalc_b2_paired(q));
     cudaEventRecord(e0, st);
     for (int r = 0; r < 2 && rc == EDB_OK; ++r)
-      rc = launch_calq64x(q->p, q->B2, q->fdf, q->partial, q->Q, st, shape, qcalc_b2_paired(q));
+      rc = launch_calq64x(q->p, q->B2, q->fin, q->fdf, q->partial, q->Q, st, shape,
+                          qcalc_b2_paired(q));
     cudaEventRecord(e1, st);
     cudaError_t ce = cudaEventSynchronize(e1);
     if (ce != cudaSuccess) {
@@ -500,8 +501,7 @@ static edb_status qcalc_fp64(edb_qcalc *q, const double2 *in, double2 *out, cuda
     return launch_calq64f(q->p, q->d.filter, q->amax, q->tc, q->bs, q->fdf, q->partial, out, st);
   }
   if (q->fp64_kernel == EDB_FP64_EMULATED && q->B2) {
-    EDB_TRY(launch_split_f(q->p.NQ, in, q->fdf, st));
-    return launch_calq64x(q->p, q->B2, q->fdf, q->partial, out, st, q->c64x_shape,
+    return launch_calq64x(q->p, q->B2, in, q->fdf, q->partial, out, st, q->c64x_shape,
                           qcalc_b2_paired(q));
   }
   return launch_calq64(q->p, q->B64, in, q->partial, out, st);

@@ -136,9 +136,10 @@ edb_status launch_split_B_paired(int N, const double *B, float2 *B2, cudaStream_
 // per table at genB).  paired: B2 is the pair table and only the l1 planes
 // with l1 <= m1 are visited.
 int calq64x_shapes();
-edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const float4 *d_fdf,
-                          double2 *d_partial, double2 *d_Q, cudaStream_t st, int shape,
-                          bool paired);
+// d_in: f-hat (FP64); d_fdf: its split (work, NQ + 1 float4), written here.
+edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const double2 *d_in,
+                          float4 *d_fdf, double2 *d_partial, double2 *d_Q, cudaStream_t st,
+                          int shape, bool paired);
 
 // Batched FP32 calQ (ALIASED): S solves, B32 the symmetric pair table in FFTW
 // order (see genB_kernel).

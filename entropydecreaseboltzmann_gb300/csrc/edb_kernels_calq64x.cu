@@ -129,6 +129,25 @@ __global__ void fdf_split_kernel(long long n, const double2 *__restrict__ f, flo
   out[i] = make_float4(rh, ih, rl, il);
 }
 
+// The output-pair kernel's input: the split of f-hat rotated along the last
+// axis by shift (see calq64p_kernel), and one zero float4 of padding.
+__global__ void fdr_split_kernel(int N, int shift, const double2 *__restrict__ f,
+                                 float4 *__restrict__ out) {
+  const long long NQ = (long long)N * N * N;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > NQ) return;
+  if (i == NQ) {
+    out[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const long long row = i / N;
+  int c = (int)(i - row * N) + shift;
+  if (c >= N) c -= N;
+  const double2 v = f[row * N + c];
+  const float rh = (float)v.x, ih = (float)v.y;
+  out[i] = make_float4(rh, ih, (float)(v.x - (double)rh), (float)(v.y - (double)ih));
+}
+
 __global__ void b2_split_kernel(long long n, const double *__restrict__ B, float2 *__restrict__ B2) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -447,29 +466,45 @@ __global__ void __launch_bounds__(MAXT, MINB)
 // B stream: ROWS table rows per ring slot (one wait, one vote and one
 // expect_tx per slot), PDEPTH rows in flight per warp.
 constexpr int PDEPTH = 8;
+struct __align__(16) P64Cursor {
+  const float4 *src;
+  int pi, i2, i3;
+  int issued;  // slot fills the warp has issued
+};
 
-template <bool TMA, int MAXT, int MINB, int ROWS>
+// fdr: f-hat split as for calq64x_kernel and rotated along the last axis by
+// the f_l shift, fdr[a1][a2][i] = f[a1][a2][(i + sL) mod N], with one float4 of
+// padding after the last row: the f_l of step i3 is entry i3 of its row (the
+// read one step ahead touches entry N, the next row's first or the padding).
+// An f_m entry x (FFTW order) sits at (x + n) mod N of its row.
+// NC > 0: N fixed at compile time (the index arithmetic folds); 0: p.N.
+template <bool TMA, int MAXT, int MINB, int ROWS, int NC>
 __global__ void __launch_bounds__(MAXT, MINB)
     calq64p_kernel(QParams p, int J2T, int LC, const float4 *__restrict__ B2p,
-                   const float4 *__restrict__ fdf, double2 *__restrict__ partial,
+                   const float4 *__restrict__ fdr, double2 *__restrict__ partial,
                    unsigned long long wait_ns) {
   constexpr int SLOTS = PDEPTH / ROWS;
   static_assert(SLOTS * ROWS == PDEPTH && RUN % ROWS == 0, "ring shape");
   extern __shared__ __align__(128) unsigned char smem64[];
-  const int N = p.N;  // == P
+  const int N = NC > 0 ? NC : p.N;  // == P
+  const int n = (N - 1) / 2;
   const int R4 = N / RUN;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nwarps = (blockDim.x + 31) >> 5;
   const int wthreads = min(32, (int)blockDim.x - warp * 32);
   const unsigned wmask = wthreads == 32 ? 0xffffffffu : ((1u << wthreads) - 1u);
-  const long long NN = (long long)N * N;
-  const long long KC2 = p.KC / 2;  // float4 per table row
-  // shared memory: [nwarps][SLOTS] mbarriers; B rings [nwarps][PDEPTH rows][32
-  // threads][2 float4]; the neighbour-pair planes (hi, then lo) [N][N] float4
+  const int NN = N * N;
+  const long long KC2 = (long long)NN * N / 2;  // float4 per table row
+  // shared memory: [nwarps][SLOTS] mbarriers; [nwarps] refill cursors; B rings
+  // [nwarps][PDEPTH rows][32 threads][2 float4]; the neighbour-pair planes (hi,
+  // then lo) [N][N] float4
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem64);
-  float4 *rings = reinterpret_cast<float4 *>(smem64 + 16 * ((nwarps * SLOTS * 8 + 15) / 16));
+  P64Cursor *curs =
+      reinterpret_cast<P64Cursor *>(smem64 + 16 * ((nwarps * SLOTS * 8 + 15) / 16));
+  float4 *rings = reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(curs) +
+                                             sizeof(P64Cursor) * nwarps);
   float4 *ehi = rings + (TMA ? (size_t)nwarps * PDEPTH * 32 * 2 : 0);
-  float4 *elo = ehi + (size_t)N * N;
+  float4 *elo = ehi + NN;
   uint64_t *mybar = bars + warp * SLOTS;
   float4 *myring = rings + (size_t)warp * PDEPTH * 32 * 2;
 
@@ -482,12 +517,12 @@ __global__ void __launch_bounds__(MAXT, MINB)
   const int j3_0 = r * RUN;
   const int chunk = blockIdx.z;
   // l1 planes this output plane visits (the pair table): a1 <= (k1 - a1) mod N
-  const int k1f = (j1 - p.n + N) % N;
+  const int k1f = (j1 - n + N) % N;
   const int plo = k1f / 2;
   const int nlist = plo + 1 + max(0, (k1f + N) / 2 - k1f);
   auto plane_i1 = [&](int pi) {
     const int a = pi <= plo ? pi : k1f + 1 + (pi - plo - 1);
-    return (a + p.n) % N;
+    return (a + n) % N;
   };
   const int NL = nlist * N;
   const int c0 = min(NL, chunk * LC), c1 = min(NL, c0 + LC);
@@ -501,18 +536,24 @@ __global__ void __launch_bounds__(MAXT, MINB)
   const long long wcol = ((long long)j1 * N + (blockIdx.y * J2T + (warp * 32) / R4)) * N +
                          ((warp * 32) % R4) * RUN;
   const uint32_t seg_bytes = (uint32_t)(wthreads * RUN * sizeof(float2));
-  const int nrows = (c1 - c0) * N;  // even: N % 4 == 0
+  const int nrows = (c1 - c0) * N;  // a multiple of 4
   bool to = false;
-  int issued = 0;  // lane 0: slot fills its warp has issued
-  int rf_pi = 0, rf_i2 = 0, rf_i3 = 0;
-  const float4 *rf_src = nullptr;  // lane 0: source of the next row to issue
-  if (TMA && lane == 0 && PDEPTH < nrows) {
-    const int t = c0 + PDEPTH / N;
-    rf_pi = t / N;
-    rf_i2 = t % N;
-    rf_i3 = PDEPTH % N;
-    const long long base = ((long long)plane_i1(rf_pi) * N + rf_i2) * N;
-    rf_src = B2p + (base + rf_i3) * KC2 + wcol / 2;
+  // lane 0's cursor (kept in shared memory, off the registers of the loop):
+  // the next row to issue as (list plane, i2, i3), its source, and the fills
+  // issued so far
+  if (TMA && lane == 0) {
+    P64Cursor c;
+    c.issued = 0;
+    c.src = nullptr;
+    c.pi = c.i2 = c.i3 = 0;
+    if (PDEPTH < nrows) {
+      const int t = c0 + PDEPTH / N;
+      c.pi = t / N;
+      c.i2 = t % N;
+      c.i3 = PDEPTH % N;
+      c.src = B2p + (((long long)plane_i1(c.pi) * N + c.i2) * N + c.i3) * KC2 + wcol / 2;
+    }
+    curs[warp] = c;
   }
 
   if (TMA) {
@@ -530,7 +571,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
           bulk_g2s(myring + (size_t)qq * 32 * 2, B2p + row_of(qq) * KC2 + wcol / 2, seg_bytes,
                    &mybar[s]);
         }
-        ++issued;
+        ++curs[warp].issued;
       }
     }
   }
@@ -539,107 +580,109 @@ __global__ void __launch_bounds__(MAXT, MINB)
 #pragma unroll
   for (int h = 0; h < 2; ++h) accR[h].h = accR[h].l = accI[h].h = accI[h].l = 0ull;
   const u64 MONE = pk(-1.0f, -1.0f);
+  const float4 *lring = myring + (size_t)lane * 2 + hsw;  // this lane's first half, ring row 0
 
-  const int x0 = (j3_0 + p.sM) % N;  // E index of pair (0, 1) at i3 = 0
-  const int fi0 = p.sL % N;
   int cur_i1 = -1;
-  int q = 0;
+  int q = 0;  // chunk row of the current group's first step (a multiple of 4)
   for (int line = c0; line < c1; ++line) {
     const int i1 = plane_i1(line / N), i2 = line % N;
-    const int a1 = (i1 + p.sL) % N, a2 = (i2 + p.sL) % N;
-    const int m2 = ((j2c - i2 + p.sM) % N + N) % N;
+    // f_l row (a1, a2) = (i + sL) mod N with sL = N - n; m = k - l for k1 = j1, k2 = j2
+    const int a1 = (i1 + N - n) % N, a2 = (i2 + N - n) % N;
+    const int m2 = (j2c - i2 + N) % N;
     if (i1 != cur_i1) {  // stage the m1-plane as neighbour pairs
       cur_i1 = i1;
-      const int m1 = ((j1 - i1 + p.sM) % N + N) % N;
-      const float4 *src = fdf + (long long)m1 * NN;
+      const int m1 = (j1 - i1 + N) % N;
+      const float4 *src = fdr + (long long)m1 * NN;
       __syncthreads();
-      for (long long e = tid; e < NN; e += blockDim.x) {
-        const long long row = e / N;
-        const int c = (int)(e - row * N);
-        const float4 v0 = src[e], v1 = src[row * N + (c + 1 == N ? 0 : c + 1)];
-        const long long d = row * N + (c & 3) * R4 + (c >> 2);
+      for (int e = tid; e < NN; e += blockDim.x) {
+        const int row = e / N;
+        const int c = e - row * N;
+        int cr = c + n;
+        if (cr >= N) cr -= N;
+        const int cr1 = cr + 1 == N ? 0 : cr + 1;
+        const float4 v0 = src[row * N + cr], v1 = src[row * N + cr1];
+        const int d = row * N + (c & 3) * R4 + (c >> 2);
         ehi[d] = make_float4(v0.x, v1.x, v0.y, v1.y);
         elo[d] = make_float4(v0.z, v1.z, v0.w, v1.w);
       }
       __syncthreads();
     }
-    const float4 *erh = ehi + (size_t)m2 * N, *erl = elo + (size_t)m2 * N;
-    const float4 *flrow = fdf + ((long long)a1 * N + a2) * N;
+    // E[x] of the row at (x mod 4) R4 + x / 4.  Step i3 = g + t reads
+    // x = (4r - i3) mod N: x / 4 = a (the group's a) at t = 0, and for t >= 1
+    // x mod 4 = 4 - t with x / 4 = (a - 1) mod R4.
+    const float4 *erh = ehi + m2 * N, *erl = elo + m2 * N;
+    const float4 *flp = fdr + ((long long)a1 * N + a2) * N;
     const long long lrow0 = ((long long)i1 * N + i2) * N;
-    // ring[s]: E entry of step i3 with i3 mod 4 = s; hi pairs (re, im), lo pairs
-    u64 eh[4][2], el[4][2];
-    auto load_e = [&](int x, int s) {
-      const int px = (x & 3) * R4 + (x >> 2);
+    u64 eh[4][2], el[4][2];  // ring[s]: E entry of step i3 with i3 mod 4 = s
+    auto load_e = [&](int px, int s) {
       const float4 u = erh[px], w = erl[px];
       eh[s][0] = pk(u.x, u.y);
       eh[s][1] = pk(u.z, u.w);
       el[s][0] = pk(w.x, w.y);
       el[s][1] = pk(w.z, w.w);
     };
-    {
-      const int x1 = x0 + 1 < N ? x0 + 1 : x0 + 1 - N;
-      const int x2 = x1 + 1 < N ? x1 + 1 : x1 + 1 - N;
-      load_e(x0, 0);
-      load_e(x1, 3);  // E[x + 1] of step 0 = the entry of step -1
-      load_e(x2, 2);  // E[x + 2] of step 0 = the entry of step -2
-    }
+    load_e(r, 0);           // x = 4r
+    load_e(R4 + r, 3);      // x = 4r + 1: E[x + 1] of step 0 = the entry of step -1
+    load_e(2 * R4 + r, 2);  // x = 4r + 2: E[x + 2] of step 0 = the entry of step -2
     const float4 *brow = B2p + lrow0 * KC2 + kcol / 2;
     float4 bv0, bv1, bn0, bn1;
     if (!TMA) {
       bv0 = __ldg(brow + hsw);
       bv1 = __ldg(brow + 1 - hsw);
     }
-    int xn = x0;
-    int fi = fi0;
-    float4 fl_next = __ldg(flrow + fi);
-    for (int g = 0; g < N; g += RUN) {
+    float4 fl_next = __ldg(flp);
+    int am = r;
+#pragma unroll 1
+    for (int g = 0; g < N; g += RUN, q += RUN) {
+      const int an = am == 0 ? R4 - 1 : am - 1;
+      const float4 *ring_g = lring + (size_t)(q & 4) * 64;  // ring row q mod 8 = (q & 4) + t
 #pragma unroll
-      for (int t = 0; t < RUN; ++t, ++q) {
-        const int i3 = g + t;
+      for (int t = 0; t < RUN; ++t) {
         if (TMA) {
-          const int slot = (q / ROWS) % SLOTS;
-          if (t % ROWS == 0) mbar_wait(&mybar[slot], (uint32_t)((q / PDEPTH) & 1), to, wait_ns);
-          const float4 *src = myring + ((size_t)(slot * ROWS + t % ROWS) * 32 + lane) * 2;
-          bv0 = src[hsw];
-          bv1 = src[1 - hsw];
+          const int slot = ((q & 4) + t) / ROWS;
+          if (t % ROWS == 0) mbar_wait(&mybar[slot], (uint32_t)((q >> 3) & 1), to, wait_ns);
+          bv0 = ring_g[t * 64];
+          bv1 = ring_g[t * 64 + 1 - 2 * hsw];
           if (t % ROWS == ROWS - 1) {
             // every lane has read the slot's rows; refill it with the next
             // ROWS rows unless a lane timed out
             const bool bad = __any_sync(wmask, to);
-            const int first = q + 1 - ROWS + PDEPTH;
+            const int first = q + t + 1 - ROWS + PDEPTH;
             if (lane == 0 && !bad && first < nrows) {
               const int nr = min(ROWS, nrows - first);
+              P64Cursor c = curs[warp];
               asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
               mbar_expect_tx(&mybar[slot], seg_bytes * nr);
               for (int rr = 0; rr < nr; ++rr) {
-                bulk_g2s(myring + ((size_t)(slot * ROWS + rr) * 32) * 2, rf_src, seg_bytes,
+                bulk_g2s(myring + ((size_t)(slot * ROWS + rr) * 32) * 2, c.src, seg_bytes,
                          &mybar[slot]);
-                if (++rf_i3 == N) {
-                  rf_i3 = 0;
-                  if (++rf_i2 == N) {
-                    rf_i2 = 0;
-                    ++rf_pi;
+                if (++c.i3 == N) {
+                  c.i3 = 0;
+                  if (++c.i2 == N) {
+                    c.i2 = 0;
+                    ++c.pi;
                   }
-                  rf_src = B2p + ((long long)plane_i1(rf_pi) * N + rf_i2) * N * KC2 + wcol / 2;
+                  c.src = B2p + ((long long)plane_i1(c.pi) * N + c.i2) * N * KC2 + wcol / 2;
                 } else {
-                  rf_src += KC2;
+                  c.src += KC2;
                 }
               }
-              ++issued;
+              ++c.issued;
+              curs[warp] = c;
             }
           }
-        } else if (i3 + 1 < N) {
-          const float4 *bn = brow + (long long)(i3 + 1) * KC2;
+        } else if (g + t + 1 < N) {
+          const float4 *bn = brow + (long long)(g + t + 1) * KC2;
           bn0 = __ldg(bn + hsw);
           bn1 = __ldg(bn + 1 - hsw);
         }
-        if (i3 > 0) {  // the new entry E[x], x = x0 - i3
-          xn = (xn == 0) ? N - 1 : xn - 1;
-          load_e(xn, t);
+        if (t == 0) {
+          if (g > 0) load_e(am, 0);
+        } else {
+          load_e((4 - t) * R4 + an, t);
         }
         const float4 fl = fl_next;
-        fi = (fi + 1 == N) ? 0 : fi + 1;
-        fl_next = __ldg(flrow + fi);
+        fl_next = __ldg(flp + g + t + 1);
         const u64 xr = pk(fl.x, fl.x), nxr = pk(-fl.x, -fl.x), nlr = pk(-fl.z, -fl.z);
         const u64 xi = pk(fl.y, fl.y), nxi = pk(-fl.y, -fl.y), nli = pk(-fl.w, -fl.w);
         const u64 li = pk(fl.w, fl.w);
@@ -664,6 +707,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
           bv1 = bn1;
         }
       }
+      am = an;
     }
   }
   if (TMA) {
@@ -673,6 +717,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
         // drain: fill f went into slot f % SLOTS, and a slot is refilled only
         // after its previous fill landed, so only each slot's last fill can
         // still be in flight
+        const int issued = curs[warp].issued;
         for (int sl = 0; sl < SLOTS && sl < issued; ++sl) {
           const int last = sl + ((issued - 1 - sl) / SLOTS) * SLOTS;
           bool t2 = false;
@@ -688,7 +733,7 @@ __global__ void __launch_bounds__(MAXT, MINB)
   for (int h = 0; h < 2; ++h) {
     const float2 Rh = upk(accR[h].h), Rl = upk(accR[h].l);
     const float2 Ih = upk(accI[h].h), Il = upk(accI[h].l);
-    double2 *o = partial + (long long)chunk * p.KC + kcol + 2 * h;
+    double2 *o = partial + (long long)chunk * NN * N + kcol + 2 * h;
     o[0] = make_double2((double)Rh.x + (double)Rl.x, (double)Ih.x + (double)Il.x);
     o[1] = make_double2((double)Rh.y + (double)Rl.y, (double)Ih.y + (double)Il.y);
   }
@@ -720,28 +765,38 @@ static_assert(sizeof(kC64pShapes) / sizeof(kC64pShapes[0]) == kC64xNShapes, "sha
 // the output-pair kernel runs the pair table when N is a multiple of 4
 static bool c64_op(const QParams &p, bool paired) { return paired && p.N % RUN == 0; }
 
+// N fixed at compile time for the output-pair kernel's tensor-copy form at
+// these sizes (0: runtime N)
+static int c64_nc(const QParams &p, bool op, bool tma) {
+  return (op && tma && (p.N == 24 || p.N == 32)) ? p.N : 0;
+}
 template <bool TMA, int S>
-static const void *c64x_fn_s(bool op) {
-  if (op)
-    return (const void *)
-        calq64p_kernel<TMA, kC64pShapes[S].maxt, kC64pShapes[S].minb, kC64pShapes[S].rows>;
+static const void *c64x_fn_s(bool op, int nc) {
+  constexpr int T = kC64pShapes[S].maxt, B = kC64pShapes[S].minb, R = kC64pShapes[S].rows;
+  if (op) {
+    if constexpr (TMA) {
+      if (nc == 24) return (const void *)calq64p_kernel<TMA, T, B, R, 24>;
+      if (nc == 32) return (const void *)calq64p_kernel<TMA, T, B, R, 32>;
+    }
+    return (const void *)calq64p_kernel<TMA, T, B, R, 0>;
+  }
   return (const void *)calq64x_kernel<TMA, kC64xShapes[S].maxt, kC64xShapes[S].minb>;
 }
 template <bool TMA>
-static const void *c64x_fn(int shape, bool op) {
+static const void *c64x_fn(int shape, bool op, int nc) {
   switch (shape) {
-    case 0: return c64x_fn_s<TMA, 0>(op);
-    case 1: return c64x_fn_s<TMA, 1>(op);
-    case 2: return c64x_fn_s<TMA, 2>(op);
-    case 3: return c64x_fn_s<TMA, 3>(op);
-    default: return c64x_fn_s<TMA, 4>(op);
+    case 0: return c64x_fn_s<TMA, 0>(op, nc);
+    case 1: return c64x_fn_s<TMA, 1>(op, nc);
+    case 2: return c64x_fn_s<TMA, 2>(op, nc);
+    case 3: return c64x_fn_s<TMA, 3>(op, nc);
+    default: return c64x_fn_s<TMA, 4>(op, nc);
   }
 }
 
 static size_t c64x_smem(int N, int threads, bool tma, bool op, int rows) {
   const int nwarps = (threads + 31) / 32;
   if (op) {
-    size_t o = 16 * (size_t)((nwarps * (PDEPTH / rows) * 8 + 15) / 16);
+    size_t o = 16 * (size_t)((nwarps * (PDEPTH / rows) * 8 + 15) / 16) + sizeof(P64Cursor) * nwarps;
     if (tma) o += 2 * sizeof(float4) * (size_t)nwarps * PDEPTH * 32;
     return o + 2 * sizeof(float4) * (size_t)N * N;
   }
@@ -792,7 +847,8 @@ static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int shape, boo
   pl.tma = aligned && (p.P % RUN) == 0 && (p.P % J2T) == 0;
   pl.smem = c64x_smem(p.N, pl.threads, pl.tma, op, kC64pShapes[shape].rows);
   int occ = 1;
-  const void *fn = pl.tma ? c64x_fn<true>(shape, op) : c64x_fn<false>(shape, op);
+  const int nc = c64_nc(p, op, pl.tma);
+  const void *fn = pl.tma ? c64x_fn<true>(shape, op, nc) : c64x_fn<false>(shape, op, nc);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, pl.threads, pl.smem);
   if (occ < 1) occ = 1;
@@ -860,12 +916,26 @@ template <bool TMA, int S>
 static void c64x_launch_s(dim3 grid, const C64xPlan &pl, const QParams &p, bool paired,
                           const float2 *d_B2, const float4 *d_fdf, double2 *d_partial,
                           cudaStream_t st) {
-  if (c64_op(p, paired))
-    calq64p_kernel<TMA, kC64pShapes[S].maxt, kC64pShapes[S].minb, kC64pShapes[S].rows>
-        <<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC,
-                                            reinterpret_cast<const float4 *>(d_B2), d_fdf,
-                                            d_partial, wait_limit_ns());
-  else
+  constexpr int T = kC64pShapes[S].maxt, B = kC64pShapes[S].minb, R = kC64pShapes[S].rows;
+  const float4 *B2p = reinterpret_cast<const float4 *>(d_B2);
+  if (c64_op(p, paired)) {
+    const int nc = c64_nc(p, true, TMA);
+    bool done = false;
+    if constexpr (TMA) {
+      if (nc == 24) {
+        calq64p_kernel<TMA, T, B, R, 24><<<grid, pl.threads, pl.smem, st>>>(
+            p, pl.J2T, pl.LC, B2p, d_fdf, d_partial, wait_limit_ns());
+        done = true;
+      } else if (nc == 32) {
+        calq64p_kernel<TMA, T, B, R, 32><<<grid, pl.threads, pl.smem, st>>>(
+            p, pl.J2T, pl.LC, B2p, d_fdf, d_partial, wait_limit_ns());
+        done = true;
+      }
+    }
+    if (!done)
+      calq64p_kernel<TMA, T, B, R, 0><<<grid, pl.threads, pl.smem, st>>>(
+          p, pl.J2T, pl.LC, B2p, d_fdf, d_partial, wait_limit_ns());
+  } else
     calq64x_kernel<TMA, kC64xShapes[S].maxt, kC64xShapes[S].minb>
         <<<grid, pl.threads, pl.smem, st>>>(p, pl.J2T, pl.LC, paired, d_B2, d_fdf, d_partial,
                                             wait_limit_ns());
@@ -883,12 +953,19 @@ static void c64x_launch(int shape, dim3 grid, const C64xPlan &pl, const QParams 
   }
 }
 
-edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const float4 *d_fdf,
-                          double2 *d_partial, double2 *d_Q, cudaStream_t st, int shape,
-                          bool paired) {
+edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const double2 *d_in,
+                          float4 *d_fdf, double2 *d_partial, double2 *d_Q, cudaStream_t st,
+                          int shape, bool paired) {
   if (shape < 0 || shape >= kC64xNShapes) shape = 0;
   if (paired && (p.P != p.N || (p.sM % p.N) != 0 || (p.sL % p.N) != p.N - p.n))
     return fail(EDB_EINVAL, "calq64x: pairs need the aliased index shifts");
+  if (c64_op(p, paired)) {
+    fdr_split_kernel<<<(unsigned)((p.NQ + 1 + 255) / 256), 256, 0, st>>>(p.N, p.sL % p.N, d_in,
+                                                                        d_fdf);
+  } else {
+    fdf_split_kernel<<<(unsigned)((p.NQ + 255) / 256), 256, 0, st>>>(p.NQ, d_in, d_fdf);
+  }
+  EDB_LAUNCHED();
   const bool aligned = ((uintptr_t)d_B2 % 16) == 0;
   if (c64_op(p, paired) && !aligned)
     return fail(EDB_EINVAL, "calq64x: the output-pair table must be 16-byte aligned");
