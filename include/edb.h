@@ -244,11 +244,13 @@ edb_status edb_set_wait_limit_ns(long long ns);
 #define EDB_FP64_ONTHEFLY 2
 edb_status edb_qcalc_set_fp64_kernel(edb_qcalc *q, int kind);
 
-/* Launch shape (CTA size and register cap) of the double-float kernel
- * (EDB_FP64_EMULATED), no reference counterpart: genB times every shape on the
- * table and keeps the fastest.  shape >= 0 overrides that choice (the results
- * do not depend on it), -1 leaves it; *current (may be NULL) receives the shape
- * in use. */
+/* Launch shape of the double-float kernel (EDB_FP64_EMULATED), no reference
+ * counterpart: CTA size and register cap, and for the output-pair form (the
+ * pair table with N % 4 == 0) the table rows per ring slot.  genB times every
+ * shape on the table and keeps the fastest.  shape >= 0 overrides that choice
+ * (shapes with another line-chunk count add the partial sums in another order:
+ * the results agree to rounding), -1 leaves it; *current (may be NULL)
+ * receives the shape in use. */
 edb_status edb_qcalc_fp64_shape(edb_qcalc *q, int shape, int *current);
 /* Number of launch shapes of the double-float kernel. */
 int edb_qcalc_fp64_shapes(void);
