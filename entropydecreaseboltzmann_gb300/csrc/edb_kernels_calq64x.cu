@@ -34,8 +34,9 @@
 // Tiling: CTA = (output plane j1, a tile of j2, all j3) x (a chunk of its
 // l-lines (i1, i2)).  Thread = (j2, run of 4 consecutive j3).  For each i1 the f-hat
 // m1-plane (m1 = j1 - i1 + sM mod N) is staged in shared memory; along i3 the
-// needed f_m slide down by one (a ring of 4).  The number of line chunks is
-// set from the measured occupancy so the grid is whole waves.  Each CTA writes
+// needed f_m slide down by one (a ring of 4).  The number of line chunks comes
+// from a model of the schedule on the measured resident CTA slots (see
+// c64x_plan_compute).  Each CTA writes
 // FP64 partial sums per chunk; calq64_reduce_kernel adds the chunks in order.
 //
 // B stream: when every warp's row segment is a contiguous, 16-byte aligned run
@@ -44,8 +45,12 @@
 // (lane 0 issues; one mbarrier per slot; waits bounded by %globaltimer, a
 // timeout sets the device status word).  Otherwise threads load their 32
 // bytes per row with __ldg, one row ahead.
+#include <algorithm>
+#include <functional>
 #include <map>
 #include <mutex>
+#include <queue>
+#include <vector>
 
 #include "edb_df.cuh"
 #include "edb_internal.cuh"
@@ -839,7 +844,7 @@ static C64xPlan c64x_plan(const QParams &p, bool aligned, int shape, bool paired
   int dev = 0;
   cudaGetDevice(&dev);
   const long long key =
-      (((((long long)dev * 128 + p.N) * 4 + p.mode) * 2 + (aligned ? 1 : 0)) * 8 + shape) * 2 +
+      (((((long long)dev * 128 + p.N) * 4 + p.mode) * 2 + (aligned ? 1 : 0)) * 16 + shape) * 2 +
       (paired ? 1 : 0);
   std::lock_guard<std::mutex> lock(mu);
   auto it = cache.find(key);
@@ -849,8 +854,13 @@ static C64xPlan c64x_plan(const QParams &p, bool aligned, int shape, bool paired
   return pl;
 }
 
-static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int shape, bool paired) {
+// shape in [0, 2 kC64xNShapes): the kernel shape shape mod kC64xNShapes, with
+// the line chunks sized by whole waves (first half) or by the schedule model
+// (second half)
+static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int shape_in, bool paired) {
   C64xPlan pl;
+  const int shape = shape_in % kC64xNShapes;
+  const bool model = shape_in >= kC64xNShapes;
   const bool op = c64_op(p, paired);
   const int R4 = (p.P + RUN - 1) / RUN;
   int J2T = std::max(1, (op ? kC64pShapes[shape].maxt : kC64xShapes[shape].maxt) / R4);
@@ -871,19 +881,51 @@ static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int shape, boo
   const int sms = device_sm_count();
   const long long wave = (long long)sms * occ;
   const long long per_chunk = (long long)p.P * tiles;
+  // l-lines each output plane j1 visits (its plane list, or all N planes)
+  std::vector<int> nlj(p.P);
+  for (int j1 = 0; j1 < p.P; ++j1) {
+    const int k1 = (j1 - p.n + p.N) % p.N;
+    nlj[j1] = paired ? (k1 / 2 + 1 + std::max(0, (k1 + p.N) / 2 - k1)) * p.N : p.N * p.N;
+  }
   const int NL = c64x_lines(p, paired);
-  // chunk count that best fills whole waves (at most 8) with balanced chunks:
-  // efficiency = useful CTA-lines / (waves * wave * lines per chunk)
+  // Whole waves: the chunk count (at most 8 waves) maximising useful CTA-lines
+  // / (waves * wave * lines per chunk), chunks sized by the longest list.
+  // Schedule model: CTAs start in launch order (j1 fastest, then the j2 tile,
+  // then the chunk) on the `wave` resident slots, each as soon as a slot
+  // frees, and cost their own lines plus a quarter line; efficiency = useful
+  // lines / (makespan * wave).  Neither predicts every table: measured at
+  // N = 24 the model's plan is 4% faster, at N = 32 3% slower (1.163 against
+  // 1.133 ms), so genB times both.
   double best_eff = -1.0;
   int best_lc = NL;
   for (int ch = 1; ch <= NL; ++ch) {
     const int lc = (NL + ch - 1) / ch;
     const int nch = (NL + lc - 1) / lc;
     if (nch != ch) continue;
-    const long long ctas = per_chunk * nch;
-    const long long waves = (ctas + wave - 1) / wave;
-    if (waves > 8) break;
-    const double eff = (double)per_chunk * NL / ((double)waves * wave * lc);
+    if (per_chunk * nch > 8 * wave) break;
+    if (!model) {
+      const long long waves = (per_chunk * nch + wave - 1) / wave;
+      const double eff = (double)per_chunk * NL / ((double)waves * wave * lc);
+      if (eff > best_eff + 1e-9) {
+        best_eff = eff;
+        best_lc = lc;
+      }
+      continue;
+    }
+    std::priority_queue<double, std::vector<double>, std::greater<double>> slots;
+    for (long long s = 0; s < wave; ++s) slots.push(0.0);
+    double useful = 0.0, makespan = 0.0;
+    for (int c = 0; c < nch; ++c)
+      for (int t = 0; t < tiles; ++t)
+        for (int j1 = 0; j1 < p.P; ++j1) {
+          const int w = std::max(0, std::min(lc, nlj[j1] - c * lc));
+          useful += w;
+          const double f = slots.top() + w + 0.25;
+          slots.pop();
+          slots.push(f);
+          makespan = std::max(makespan, f);
+        }
+    const double eff = useful / (makespan * (double)wave);
     if (eff > best_eff + 1e-9) {
       best_eff = eff;
       best_lc = lc;
@@ -897,7 +939,7 @@ static C64xPlan c64x_plan_compute(const QParams &p, bool aligned, int shape, boo
 int calq64x_nchunk(const QParams &p, int *J2T_out) {
   // upper bound over the variants, used to size the partial-sum buffer
   int n = 1;
-  for (int shape = 0; shape < kC64xNShapes; ++shape)
+  for (int shape = 0; shape < 2 * kC64xNShapes; ++shape)
     for (int al = 0; al <= 1; ++al)
       for (int pa = 0; pa <= 1; ++pa) {
         const C64xPlan pl = c64x_plan(p, al != 0, shape, pa != 0);
@@ -926,7 +968,7 @@ edb_status launch_split_B_paired(int N, const double *B, float2 *B2, cudaStream_
   return EDB_OK;
 }
 
-int calq64x_shapes() { return kC64xNShapes; }
+int calq64x_shapes() { return 2 * kC64xNShapes; }
 
 template <bool TMA, int S>
 static void c64x_launch_s(dim3 grid, const C64xPlan &pl, const QParams &p, bool paired,
@@ -972,7 +1014,7 @@ static void c64x_launch(int shape, dim3 grid, const C64xPlan &pl, const QParams 
 edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const double2 *d_in,
                           float4 *d_fdf, double2 *d_partial, double2 *d_Q, cudaStream_t st,
                           int shape, bool paired) {
-  if (shape < 0 || shape >= kC64xNShapes) shape = 0;
+  if (shape < 0 || shape >= 2 * kC64xNShapes) shape = 0;
   if (paired && (p.P != p.N || (p.sM % p.N) != 0 || (p.sL % p.N) != p.N - p.n))
     return fail(EDB_EINVAL, "calq64x: pairs need the aliased index shifts");
   if (c64_op(p, paired)) {
@@ -988,9 +1030,9 @@ edb_status launch_calq64x(const QParams &p, const float2 *d_B2, const double2 *d
   const C64xPlan pl = c64x_plan(p, aligned, shape, paired);
   dim3 grid((unsigned)p.P, (unsigned)pl.tiles, (unsigned)pl.nch);
   if (pl.tma)
-    c64x_launch<true>(shape, grid, pl, p, paired, d_B2, d_fdf, d_partial, st);
+    c64x_launch<true>(shape % kC64xNShapes, grid, pl, p, paired, d_B2, d_fdf, d_partial, st);
   else
-    c64x_launch<false>(shape, grid, pl, p, paired, d_B2, d_fdf, d_partial, st);
+    c64x_launch<false>(shape % kC64xNShapes, grid, pl, p, paired, d_B2, d_fdf, d_partial, st);
   EDB_LAUNCHED();
   return launch_calq64_reduce(p, pl.nch, d_partial, d_Q, st);
 }

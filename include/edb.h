@@ -245,9 +245,11 @@ edb_status edb_set_wait_limit_ns(long long ns);
 edb_status edb_qcalc_set_fp64_kernel(edb_qcalc *q, int kind);
 
 /* Launch shape of the double-float kernel (EDB_FP64_EMULATED), no reference
- * counterpart: CTA size and register cap, and for the output-pair form (the
- * pair table with N % 4 == 0) the table rows per ring slot.  genB times every
- * shape on the table and keeps the fastest.  shape >= 0 overrides that choice
+ * counterpart: CTA size and register cap, for the output-pair form (the pair
+ * table with N % 4 == 0) the table rows per ring slot, and the rule that sizes
+ * the l-line chunks (the second half of the shapes repeats the first with
+ * chunks from a model of the schedule).  genB times every shape on the table
+ * and keeps the fastest.  shape >= 0 overrides that choice
  * (shapes with another line-chunk count add the partial sums in another order:
  * the results agree to rounding), -1 leaves it; *current (may be NULL)
  * receives the shape in use. */
