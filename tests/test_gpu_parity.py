@@ -345,7 +345,8 @@ def test_fp64_emulated_kernel_matches_native_and_oracle(edb, oracle, N, mode):
             assert rel_l2(Qe[modes], Qd) <= 1e-12
             assert rel_l2(Qn[modes], Qd) <= 1e-12
         # every launch shape of the double-float kernel (CTA size, register
-        # cap; the l-line chunking follows the shape) meets the same bound
+        # cap, rows per ring slot, and either rule for the l-line chunks)
+        # meets the same bound
         q.set_fp64_kernel(0)
         for shp in range(edb.lib.edb_qcalc_fp64_shapes()):
             q.fp64_shape(shp)
