@@ -449,10 +449,16 @@ def main():
             frac = {0: visited, 1: 1.0, 2: 0.0}[kind]
             n2 = 3 * (2 * (Nf - 1 - (Nf - 1) // 2)) ** 2  # largest squared norm (genB's amax)
             table = {0: nb, 1: nb, 2: (n2 + 1) * (n2 // 4 + 1) * 8 + Nf ** 3 * 16}[kind]
+            # the kernel each kind runs on this ALIASED table (the double-float
+            # one in the launch shape genB timed fastest)
+            kern = {0: "calq64p_kernel" if Nf % 4 == 0 else "calq64x_kernel",
+                    1: "calq64_kernel", 2: "calq64f_kernel"}[kind]
             res[name] = {"evals_per_s": 1.0 / t, "ms_per_eval": t * 1e3,
                          "B_stream_GBs": nb / t / 1e9,
                          "B_read_GBs": nb * frac / t / 1e9,
-                         "table_bytes": table}
+                         "table_bytes": table, "kernel": kern}
+            if kind == 0:
+                res[name]["launch_shape"] = q64.fp64_shape()
         fp64[f"N{Nf}"] = res
         del q64
     peaks, peak_src = measured_peaks()
